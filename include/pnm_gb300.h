@@ -1,0 +1,136 @@
+/* pnm_gb300 — GB300-native (sm_103a) pore-network extraction: the C ABI.
+ *
+ * Drop-in replacement for the single-rank path of peclet.pnm (reference: src/pore_extraction.hpp
+ * and its nanobind binding src/pnm_bindings.cpp). All array arguments are plain pointers:
+ *   - volumes are flat x-fastest arrays of nx*ny*nz elements (== zyx C-order (Nz,Ny,Nx));
+ *   - origin / spacing are xyz float32 triples (the binding's zyx doubles, reversed and cast);
+ *   - grad_p is an xyz float64 triple;
+ *   - the SDF is float32 and negative inside the solid.
+ * Every function returns a status (PNM_OK = 0); pnm_last_error(ctx) holds the message of the last
+ * failure on that context. Functions are thread-safe across distinct contexts; one context must
+ * not be used by two threads at once. Host-pointer entry points copy inputs to the device and
+ * results back; *_dev entry points take device pointers and leave results on the device.
+ *
+ * Limits: nx*ny*nz < 2^31 - 3 (voxel ids and labels are int32, as in the reference's get_idx);
+ * extract_network_flow additionally needs 3*nx*ny*nz < 2^31 (face ids are compacted to int32).
+ */
+#ifndef PNM_GB300_H
+#define PNM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PNM_OK 0
+#define PNM_ERR_ARG 1           /* null pointer, non-positive dims or spacing, partial openness */
+#define PNM_ERR_SHAPE 2         /* volume too large for int32 voxel ids / int32 face ids */
+#define PNM_ERR_CAPACITY 3      /* a caller-provided device output is too small; the count
+                                   argument receives the required size */
+#define PNM_ERR_NOT_CONVERGED 4 /* a bounded device fixpoint / wait hit its iteration limit */
+#define PNM_ERR_CUDA 5          /* a CUDA runtime call failed */
+#define PNM_ERR_NO_DEVICE 6     /* no CUDA device, or the device is not sm_103 */
+#define PNM_ERR_INTERNAL 7
+
+/* struct Pore (pore_extraction.hpp:24-26): world position of the refined SDF peak and its value. */
+typedef struct {
+  float x, y, z, radius;
+} pnm_pore;
+
+typedef struct pnm_ctx pnm_ctx;
+
+/* Context: owns the device, a CUDA stream, a grow-only device workspace and the error message.
+ * Replaces the reference's global Kokkos::initialize / per-call View allocation
+ * (pnm_bindings.cpp:73-84). device < 0 picks the current device. */
+int pnm_ctx_create(int device, pnm_ctx** out);
+void pnm_ctx_destroy(pnm_ctx* ctx);
+const char* pnm_last_error(const pnm_ctx* ctx);
+/* Use a caller-owned cudaStream_t (passed as void*) for all work of this context; NULL restores
+ * the context's own stream. */
+int pnm_ctx_set_stream(pnm_ctx* ctx, void* stream);
+/* Releases the workspace (it regrows on the next call). */
+int pnm_ctx_trim(pnm_ctx* ctx);
+/* Name of the execution space (the reference exposes Kokkos' backend name as
+ * `execution_space`, pnm_bindings.cpp:83). */
+const char* pnm_execution_space(void);
+/* Frees buffers returned by the host entry points. */
+void pnm_free(void* p);
+
+/* ---- host-pointer entry points ------------------------------------------------------------ */
+
+/* extract_pores (pore_extraction.hpp:143 extract_pores_k; binding pnm_bindings.cpp:110-121).
+ * Pores are the SDF voxels whose (value, wrapped index) is a strict maximum over their 26
+ * periodic neighbours, refined by the SDF^2-weighted 27-point centroid. Returned in voxel-index
+ * order (the reference's order is an atomic race); at most 1e6, the first in voxel order.
+ * *pores is allocated by the library (pnm_free); *n_pores receives the count. */
+int pnm_extract_pores(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t ny, int32_t nz,
+                      const float origin_xyz[3], const float spacing_xyz[3], pnm_pore** pores,
+                      int64_t* n_pores);
+
+/* segment_volume (pore_extraction.hpp:389 segment_volume_k; pnm_bindings.cpp:123-132).
+ * Writes the flat per-voxel labels: pores 1,2,... (gradient-ascent basins), solid -1,-2,...
+ * (marker CCL + Jacobi flood), debris 0. seg has nx*ny*nz int32 elements. */
+int pnm_segment_volume(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t ny, int32_t nz,
+                       const float spacing_xyz[3], int32_t* seg);
+
+/* extract_topology_gpu (pore_extraction.hpp:454 extract_topology_k; pnm_bindings.cpp:134-140).
+ * Unique (min, max) label pairs across the +x/+y/+z periodic faces, sorted lexicographically.
+ * *pairs (2 * n_pairs int32, interleaved) is allocated by the library (pnm_free). */
+int pnm_extract_topology(pnm_ctx* ctx, const int32_t* seg, int32_t nx, int32_t ny, int32_t nz,
+                         int32_t** pairs, int64_t* n_pairs);
+
+/* extract_pore_network (pore_extraction.hpp:1011 extract_pore_network_k;
+ * pnm_bindings.cpp:143-157): pores, seg (caller buffer, nx*ny*nz) and pairs in one pass over a
+ * device-resident SDF. */
+int pnm_extract_pore_network(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t ny, int32_t nz,
+                             const float origin_xyz[3], const float spacing_xyz[3],
+                             pnm_pore** pores, int64_t* n_pores, int32_t* seg, int32_t** pairs,
+                             int64_t* n_pairs);
+
+/* Result of extract_network_flow (struct NetworkFlow, pore_extraction.hpp:482-491). */
+typedef struct {
+  int64_t n_pores, n_throats;
+  pnm_pore* pores;       /* by label: pores[k] <-> label k+1 */
+  double* pore_pressure; /* n_pores */
+  double* pore_residual; /* n_pores */
+  int32_t* throats;      /* 2 * n_throats, (li < lj) interleaved; a pair may repeat */
+  double* throat_flow;   /* n_throats, positive li -> lj */
+  double* throat_area;   /* n_throats */
+  double* throat_dp;     /* n_throats */
+} pnm_flow_result;
+
+/* extract_network_flow (pore_extraction.hpp:493 extract_network_flow_k;
+ * pnm_bindings.cpp:162-209). u, v, w, p: float64 MAC fields on the SDF grid (u(i,j,k) on the -x
+ * face of cell (i,j,k)); ox, oy, oz: openness, all three or none (NULL = fully open).
+ * FP64 sums are accumulated exactly (128-bit fixed point), so results are deterministic.
+ * *out is allocated by the library (pnm_flow_result_free). */
+int pnm_extract_network_flow(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t ny, int32_t nz,
+                             const float origin_xyz[3], const float spacing_xyz[3],
+                             const double* u, const double* v, const double* w, const double* p,
+                             const double* ox, const double* oy, const double* oz,
+                             const double grad_p_xyz[3], pnm_flow_result** out);
+void pnm_flow_result_free(pnm_flow_result* r);
+
+/* ---- device-pointer entry points (resident / serving path) -------------------------------- */
+
+/* extract_pore_network on a device SDF. Outputs are device buffers: d_pores (pore_cap entries),
+ * d_seg (nx*ny*nz), d_pairs (2 * pair_cap int32). Counts are returned to the host. If a count
+ * exceeds its cap, returns PNM_ERR_CAPACITY with the count set to the required size and the
+ * first `cap` entries written. d_seg may be NULL (labels not needed). */
+int pnm_extract_pore_network_dev(pnm_ctx* ctx, const float* d_sdf, int32_t nx, int32_t ny,
+                                 int32_t nz, const float origin_xyz[3], const float spacing_xyz[3],
+                                 pnm_pore* d_pores, int64_t pore_cap, int64_t* n_pores,
+                                 int32_t* d_seg, int32_t* d_pairs, int64_t pair_cap,
+                                 int64_t* n_pairs);
+
+/* segment_volume on a device SDF into a device seg buffer. */
+int pnm_segment_volume_dev(pnm_ctx* ctx, const float* d_sdf, int32_t nx, int32_t ny, int32_t nz,
+                           const float spacing_xyz[3], int32_t* d_seg);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PNM_GB300_H */

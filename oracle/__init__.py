@@ -184,6 +184,8 @@ class Oracle:
         ptr = [x.ctypes.data_as(_vp) if x is not None else None for x in f]
         r = self._f_flow(a.ctypes.data_as(_vp), _i(nx), _i(ny), _i(nz), o.ctypes.data_as(_vp),
                          s.ctypes.data_as(_vp), *ptr, g.ctypes.data_as(_vp), *self._targs())
+        if not r:
+            raise RuntimeError("extract_network_flow failed in the reference implementation")
         c = r.contents
         npo, nt = c.n_pores, c.n_throats
         out = {

@@ -111,10 +111,15 @@ ref_flow_result* ref_extract_network_flow(const float* sdf, int nx, int ny, int 
                                           const double* ox, const double* oy, const double* oz,
                                           const double* grad_p) {
   const std::size_t n = std::size_t(nx) * ny * nz;
-  auto net = pnm::extract_network_flow_k(
+  pnm::NetworkFlow net;
+  try {  // max label < 0 makes the reference size a view with a negative count (undefined)
+    net = pnm::extract_network_flow_k(
       vec(sdf, n), {nx, ny, nz}, {org[0], org[1], org[2]}, {spc[0], spc[1], spc[2]}, vecd(u, n),
       vecd(v, n), vecd(w, n), vecd(p, n), vecd(ox, n), vecd(oy, n), vecd(oz, n),
       {grad_p[0], grad_p[1], grad_p[2]});
+  } catch (...) {
+    return nullptr;
+  }
   auto* r = static_cast<ref_flow_result*>(std::calloc(1, sizeof(ref_flow_result)));
   r->n_pores = (long long)net.pores.size();
   r->n_throats = (long long)net.throats.size();

@@ -1,0 +1,157 @@
+"""ctypes binding of libpnm_gb300.so (the C ABI declared in include/pnm_gb300.h).
+
+The shared library must have been built (``peclet_pnm_gb300.build.build()``); there is no
+fallback implementation, so importing this module without it raises ImportError.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpnm_gb300.so")
+
+PNM_OK = 0
+PNM_ERR_ARG = 1
+PNM_ERR_SHAPE = 2
+PNM_ERR_CAPACITY = 3
+PNM_ERR_NOT_CONVERGED = 4
+PNM_ERR_CUDA = 5
+PNM_ERR_NO_DEVICE = 6
+PNM_ERR_INTERNAL = 7
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError(f"{LIB_PATH} is not built; run `python -m peclet_pnm_gb300.build` "
+                      "(no CPU fallback exists)")
+
+lib = ctypes.CDLL(LIB_PATH)
+
+_P = ctypes.POINTER
+_vp = ctypes.c_void_p
+_i32 = ctypes.c_int32
+_i64 = ctypes.c_int64
+
+
+class PnmPore(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_float), ("y", ctypes.c_float), ("z", ctypes.c_float),
+                ("radius", ctypes.c_float)]
+
+
+class PnmFlowResult(ctypes.Structure):
+    _fields_ = [("n_pores", _i64), ("n_throats", _i64), ("pores", _P(PnmPore)),
+                ("pore_pressure", _P(ctypes.c_double)), ("pore_residual", _P(ctypes.c_double)),
+                ("throats", _P(ctypes.c_int32)), ("throat_flow", _P(ctypes.c_double)),
+                ("throat_area", _P(ctypes.c_double)), ("throat_dp", _P(ctypes.c_double))]
+
+
+def _sig(name, res, *args):
+    f = getattr(lib, name)
+    f.restype = res
+    f.argtypes = list(args)
+    return f
+
+
+pnm_ctx_create = _sig("pnm_ctx_create", ctypes.c_int, ctypes.c_int, _P(_vp))
+pnm_ctx_destroy = _sig("pnm_ctx_destroy", None, _vp)
+pnm_last_error = _sig("pnm_last_error", ctypes.c_char_p, _vp)
+pnm_ctx_set_stream = _sig("pnm_ctx_set_stream", ctypes.c_int, _vp, _vp)
+pnm_ctx_trim = _sig("pnm_ctx_trim", ctypes.c_int, _vp)
+pnm_execution_space = _sig("pnm_execution_space", ctypes.c_char_p)
+pnm_free = _sig("pnm_free", None, _vp)
+pnm_extract_pores = _sig("pnm_extract_pores", ctypes.c_int, _vp, _vp, _i32, _i32, _i32, _vp, _vp,
+                         _P(_P(PnmPore)), _P(_i64))
+pnm_segment_volume = _sig("pnm_segment_volume", ctypes.c_int, _vp, _vp, _i32, _i32, _i32, _vp,
+                          _vp)
+pnm_segment_volume_dev = _sig("pnm_segment_volume_dev", ctypes.c_int, _vp, _vp, _i32, _i32, _i32,
+                              _vp, _vp)
+pnm_extract_topology = _sig("pnm_extract_topology", ctypes.c_int, _vp, _vp, _i32, _i32, _i32,
+                            _P(_P(ctypes.c_int32)), _P(_i64))
+pnm_extract_pore_network = _sig("pnm_extract_pore_network", ctypes.c_int, _vp, _vp, _i32, _i32,
+                                _i32, _vp, _vp, _P(_P(PnmPore)), _P(_i64), _vp,
+                                _P(_P(ctypes.c_int32)), _P(_i64))
+pnm_extract_pore_network_dev = _sig("pnm_extract_pore_network_dev", ctypes.c_int, _vp, _vp, _i32,
+                                    _i32, _i32, _vp, _vp, _vp, _i64, _P(_i64), _vp, _vp, _i64,
+                                    _P(_i64))
+pnm_extract_network_flow = _sig("pnm_extract_network_flow", ctypes.c_int, _vp, _vp, _i32, _i32,
+                                _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                _P(_P(PnmFlowResult)))
+pnm_flow_result_free = _sig("pnm_flow_result_free", None, _P(PnmFlowResult))
+
+#: every symbol include/pnm_gb300.h declares
+EXPORTED = ["pnm_ctx_create", "pnm_ctx_destroy", "pnm_last_error", "pnm_ctx_set_stream",
+            "pnm_ctx_trim", "pnm_execution_space", "pnm_free", "pnm_extract_pores",
+            "pnm_segment_volume", "pnm_extract_topology", "pnm_extract_pore_network",
+            "pnm_extract_network_flow", "pnm_flow_result_free", "pnm_extract_pore_network_dev",
+            "pnm_segment_volume_dev"]
+
+
+class PnmError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(msg)
+        self.code = code
+
+
+class Context:
+    """One pnm_ctx (device, stream, workspace). Not shared between threads."""
+
+    def __init__(self, device: int = -1):
+        h = _vp()
+        rc = pnm_ctx_create(int(device), ctypes.byref(h))
+        if rc != PNM_OK:
+            raise PnmError(rc, {PNM_ERR_NO_DEVICE: "no sm_103 CUDA device available",
+                                PNM_ERR_CUDA: "CUDA initialisation failed"}.get(
+                rc, f"pnm_ctx_create failed ({rc})"))
+        self.h = h
+
+    def check(self, rc: int):
+        if rc != PNM_OK:
+            msg = pnm_last_error(self.h).decode(errors="replace")
+            raise PnmError(rc, msg or f"pnm error {rc}")
+
+    def set_stream(self, stream_ptr: int | None):
+        self.check(pnm_ctx_set_stream(self.h, stream_ptr or None))
+
+    def trim(self):
+        self.check(pnm_ctx_trim(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            pnm_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_tls = threading.local()
+
+
+def default_context() -> Context:
+    """The calling thread's context on the current device (created on first use)."""
+    ctx = getattr(_tls, "ctx", None)
+    if ctx is None:
+        ctx = Context(-1)
+        _tls.ctx = ctx
+    return ctx
+
+
+def as_ptr(a: np.ndarray):
+    return a.ctypes.data_as(_vp)
+
+
+def take_array(ptr, count: int, dtype, free: bool = True) -> np.ndarray:
+    """Copies a library-allocated host buffer into numpy and frees it."""
+    if count > 0:
+        out = np.ctypeslib.as_array(ctypes.cast(ptr, _P(np.ctypeslib.as_ctypes_type(dtype))),
+                                    (int(count),)).copy()
+    else:
+        out = np.zeros((0,), dtype)
+    if free and ptr:
+        pnm_free(ctypes.cast(ptr, _vp))
+    return out

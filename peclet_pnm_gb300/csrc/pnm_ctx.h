@@ -1,0 +1,156 @@
+// Host-side internals shared by the translation units of libpnm_gb300.so: the context, its
+// grow-only device workspace, the device counter block, and the stage entry points that the C
+// ABI (pnm_capi.cu) sequences.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "pnm_gb300.h"
+
+namespace pnm {
+
+// ---- status plumbing ---------------------------------------------------------------------------
+struct Status {
+  int code = PNM_OK;
+  std::string msg;
+  static Status ok() { return {}; }
+  bool good() const { return code == PNM_OK; }
+};
+#define PNM_TRY(expr)            \
+  do {                           \
+    ::pnm::Status _s = (expr);   \
+    if (!_s.good()) return _s;   \
+  } while (0)
+Status cuda_status(cudaError_t e, const char* what);
+#define PNM_CUDA(call)                                              \
+  do {                                                              \
+    cudaError_t _e = (call);                                        \
+    if (_e != cudaSuccess) return ::pnm::cuda_status(_e, #call);    \
+  } while (0)
+
+// ---- device error flags (set by kernels instead of trapping; read back by the host) -------------
+enum ErrFlag : unsigned {
+  ERRF_UF_LIMIT = 1u,       // a union-find find/unite exceeded its iteration limit
+  ERRF_HASH_FULL = 2u,      // the pair hash set ran out of probes
+  ERRF_FLOOD_LIMIT = 4u,    // the flood wavefront exceeded its sweep limit
+  ERRF_FACE_LIMIT = 8u,     // a face-CCL find/unite exceeded its iteration limit
+};
+
+// ---- counter block (device ints; one copy per context) ------------------------------------------
+enum Counter : int {
+  CNT_ERR = 0,
+  CNT_KEYS,          // distinct basin / solid keys seen (keylist length)
+  CNT_FRONT0,        // flood frontier length, ping
+  CNT_FRONT1,        // flood frontier length, pong
+  CNT_FRONT_SPARE,
+  CNT_FACE_REC,      // network flow: emitted flux records
+  CNT_FLOW_SPARE0,
+  CNT_FLOW_SPARE1,
+  CNT_COUNT = 32
+};
+
+// ---- grow-only device workspace ---------------------------------------------------------------
+enum Slot : int {
+  S_SDF = 0, S_CODE, S_L, S_KEY, S_IDTAB, S_SEG, S_FRONT0, S_FRONT1, S_TMP, S_KEYLIST,
+  S_PEAKBITS, S_PEAKPREF, S_FIRSTP, S_FIRSTS, S_PREFP, S_PREFS, S_SCAN0, S_SCAN1,
+  S_HASH, S_KEYS_A, S_KEYS_B, S_VALS_A, S_VALS_B, S_RSHIST, S_PORES, S_PAIRS, S_SEGIN,
+  // network flow
+  S_U, S_V, S_W, S_P, S_OX, S_OY, S_OZ, S_FLOWLAB, S_FBITS, S_FCORE, S_FPREF, S_FID, S_FPAIR,
+  S_FPAR, S_FFILM, S_FMINCORE, S_FLABEL, S_ROOTFLAG, S_SLOTOF, S_PEAK, S_NPORES_OUT,
+  S_PPRES, S_REC, S_ACC, S_TDP, S_THROATS, S_MAXBITS, S_FLOWOUT,
+  S_COUNT
+};
+
+struct Workspace {
+  std::vector<void*> ptr = std::vector<void*>(S_COUNT, nullptr);
+  std::vector<size_t> cap = std::vector<size_t>(S_COUNT, 0);
+  // Returns a device buffer of at least `bytes` for `slot` (grow-only; contents undefined).
+  Status get(int slot, size_t bytes, void** out);
+  void release();
+  size_t total_bytes() const;
+};
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  Workspace ws;
+  unsigned* d_cnt = nullptr;  // CNT_COUNT device counters
+  unsigned* h_cnt = nullptr;  // pinned host mirror
+  int sm_count = 0;
+  std::string last_error;
+  Status fail(Status s) {
+    last_error = s.msg;
+    return s;
+  }
+  template <class T>
+  Status buf(int slot, size_t count, T** out) {
+    void* p = nullptr;
+    Status s = ws.get(slot, count * sizeof(T) + 16, &p);
+    *out = static_cast<T*>(p);
+    return s;
+  }
+  Status read_counters();  // synchronises the stream and copies d_cnt -> h_cnt
+};
+
+#ifdef __CUDACC__
+#define PNM_HD __host__ __device__
+#else
+#define PNM_HD
+#endif
+struct Dims {
+  int nx, ny, nz;
+  PNM_HD long long n() const { return (long long)nx * ny * nz; }
+};
+
+// Validates dims (positive, n < 2^31 - 3) and spacing (finite, > 0).
+Status check_dims(Dims d, const float* spacing, bool need_spacing);
+
+// ---- stages (pnm_segment.cu) -------------------------------------------------------------------
+// Everything below runs on ctx.stream over a device SDF; results stay in the workspace.
+
+struct SegState {
+  Dims d;
+  const float* sdf = nullptr;
+  uint8_t* code = nullptr;      // per voxel: ascent direction (5 bits), class (2), flood-seed (1)
+  int32_t* key = nullptr;       // per voxel: basin root (>=0), ~solid label (<0), INT_MIN none
+  int32_t* idtab = nullptr;     // per key voxel: final signed label id
+  uint32_t* peakbits = nullptr; // bitmap of extract_pores peaks
+  int n_pore_labels = 0;        // np
+  int n_solid_labels = 0;
+  int flood_sweeps = 0;
+};
+
+// Fused SDF pass + CCL + flood + gradient roots + first-appearance renumbering.
+Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st);
+// Writes seg (if d_seg != null) and the unique sorted label pairs (if want_pairs) from the state.
+Status run_seg_and_topology(Ctx& c, const SegState& st, int32_t* d_seg, bool want_pairs,
+                            int32_t** d_pairs_out, int64_t* n_pairs);
+// Topology of a caller-provided device seg.
+Status run_topology_of_seg(Ctx& c, const int32_t* d_seg, Dims d, int32_t** d_pairs_out,
+                           int64_t* n_pairs);
+// Compacts the peak bitmap into pores (voxel order, centroid-refined) in d_out (cap entries).
+Status run_pores(Ctx& c, const SegState& st, const float origin[3], const float spacing[3],
+                 pnm_pore* d_out, int64_t cap, int64_t* n_pores);
+// SDF pass only (for extract_pores alone).
+Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st);
+
+// ---- network flow (pnm_flow.cu) ------------------------------------------------------------
+struct FlowInputs {
+  const double *u, *v, *w, *p, *ox, *oy, *oz;  // device pointers; o* may be null
+  double grad_p[3];
+};
+struct FlowOutputsHost {
+  std::vector<pnm_pore> pores;
+  std::vector<double> pore_pressure, pore_residual, throat_flow, throat_area, throat_dp;
+  std::vector<int32_t> throats;
+};
+Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const float spacing[3],
+                        const FlowInputs& in, FlowOutputsHost* out);
+
+}  // namespace pnm

@@ -1,0 +1,841 @@
+// Network flow on the segmentation: basin peaks and pore centres, trilinear pore pressures,
+// flow basins (gradient ascent from every cell), per-patch throats by a two-tier CCL over the
+// compacted interface faces, openness-weighted MAC face fluxes, and throat pressure drops.
+//
+// Reference: src/pore_extraction.hpp:493-997 (extract_network_flow_k), cited per kernel.
+//
+// FP64 sums (pore_residual, throat_flow, throat_area, throat centroid moments) are accumulated
+// EXACTLY: every term is converted to a 128-bit two's-complement fixed-point integer at a common
+// power-of-two scale chosen from a bound on the terms, and integer atomics add them. Integer
+// addition is associative, so the sums are independent of thread order (deterministic), and the
+// only rounding is the final conversion back to double (correctly rounded). The reference's
+// atomic double sums carry order-dependent rounding; they agree with these to their own rounding
+// error.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include "pnm_ctx.h"
+#include "pnm_device.cuh"
+
+namespace pnm {
+
+namespace {
+
+__device__ __forceinline__ int3 coords_of(long long v, int nx, int ny) {
+  return make_int3((int)(v % nx), (int)((v / nx) % ny), (int)(v / ((long long)nx * ny)));
+}
+__device__ __forceinline__ int pmod(int v, int n) {
+  const int r = v % n;
+  return r < 0 ? r + n : r;
+}
+
+// ---- exact 128-bit fixed-point accumulation --------------------------------------------------
+struct I128 {
+  unsigned long long lo;
+  long long hi;
+};
+__device__ __forceinline__ I128 to_fixed(double x, int scale) {
+  I128 r{0ull, 0ll};
+  if (x == 0.0 || !isfinite(x)) return r;
+  const double y = scalbn(x, scale);  // exact power-of-two scaling
+  const double a = fabs(y);
+  unsigned long long mlo;
+  long long mhi;
+  if (a < 9223372036854775808.0) {  // < 2^63
+    mlo = (unsigned long long)a;    // truncation toward zero
+    mhi = 0;
+  } else {
+    int e;
+    const double fr = frexp(a, &e);  // a = fr * 2^e, fr in [0.5, 1)
+    const unsigned long long m = (unsigned long long)scalbn(fr, 53);  // 53-bit integer mantissa
+    const int sh = min(e - 53, 73);  // >= 10 here; < 42 by the chosen scale (clamp: no UB)
+    if (sh >= 64) {
+      mlo = 0;
+      mhi = (long long)(m << (sh - 64));
+    } else {
+      mlo = m << sh;
+      mhi = (long long)(m >> (64 - sh));
+    }
+  }
+  if (y < 0) {  // two's complement negate
+    mlo = ~mlo + 1ull;
+    mhi = ~mhi + (mlo == 0 ? 1 : 0);
+  }
+  r.lo = mlo;
+  r.hi = mhi;
+  return r;
+}
+__device__ __forceinline__ I128 add128(I128 a, I128 b) {
+  I128 r;
+  r.lo = a.lo + b.lo;
+  r.hi = a.hi + b.hi + (r.lo < a.lo ? 1 : 0);
+  return r;
+}
+__device__ __forceinline__ void atomic_add128(unsigned long long* acc, I128 v) {
+  if (v.lo == 0 && v.hi == 0) return;
+  const unsigned long long old = atomicAdd(&acc[0], v.lo);
+  const unsigned long long carry = (old + v.lo < old) ? 1ull : 0ull;
+  const unsigned long long hi = (unsigned long long)v.hi + carry;
+  if (hi) atomicAdd(&acc[1], hi);
+}
+// Sums the I128 values of the lanes sharing `target` (>= 0) and lets the lowest such lane add the
+// group total to acc[2*target]. Exact, so the grouping does not affect the result.
+__device__ __forceinline__ void warp_accumulate(unsigned long long* acc, int target, I128 v) {
+  const unsigned peers = __match_any_sync(0xffffffffu, target);
+  I128 s{0ull, 0ll};
+#pragma unroll 4
+  for (int j = 0; j < 32; ++j) {
+    I128 o;
+    o.lo = __shfl_sync(0xffffffffu, v.lo, j);
+    o.hi = __shfl_sync(0xffffffffu, v.hi, j);
+    if ((peers >> j) & 1u) s = add128(s, o);
+  }
+  if (target >= 0 && (__ffs(peers) - 1) == (int)lane_id()) atomic_add128(&acc[2 * (long long)target], s);
+}
+__device__ __forceinline__ double from_fixed(unsigned long long lo, long long hi, int scale) {
+  const bool neg = hi < 0;
+  unsigned long long mlo = lo, mhi = (unsigned long long)hi;
+  if (neg) {
+    mlo = ~mlo + 1ull;
+    mhi = ~mhi + (mlo == 0 ? 1ull : 0ull);
+  }
+  double d;
+  if (mhi == 0) {
+    d = (double)mlo;  // correctly rounded u64 -> double
+  } else {
+    const int sh = 64 - __clzll((long long)mhi);  // bits of mhi
+    unsigned long long top = (mhi << (64 - sh)) | (mlo >> sh);
+    if (mlo & ((1ull << sh) - 1ull)) top |= 1ull;  // sticky bit for correct rounding
+    d = scalbn((double)top, sh);
+  }
+  d = scalbn(d, -scale);
+  return neg ? -d : d;
+}
+
+__device__ __forceinline__ void atomic_max_abs(unsigned long long* slot, double v) {
+  const double a = fabs(v);
+  if (!(a > 0.0) || !isfinite(a)) return;
+  atomicMax(slot, (unsigned long long)__double_as_longlong(a));
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// =============================================================================================
+// kernels
+// =============================================================================================
+
+// basin peaks (pore_extraction.hpp:527-533): a pore voxel that is its own ascent target is the
+// root of its basin; peak[label-1] = voxel. Labels whose root is a walk capped at 512 steps have
+// no peak and keep 0 (the zero-initialised view).
+__global__ void k_peaks(const uint32_t* __restrict__ peakbits, long long words,
+                        const uint8_t* __restrict__ code, const int* __restrict__ seg,
+                        int* __restrict__ peak) {
+  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < words;
+       w += (long long)gridDim.x * blockDim.x) {
+    uint32_t b = peakbits[w];
+    while (b) {
+      const int j = __ffs(b) - 1;
+      b &= b - 1;
+      const long long v = w * 32 + j;
+      if (code_cls(code[v]) == CLS_PORE) peak[seg[v] - 1] = (int)v;
+    }
+  }
+}
+
+// pore centres (:534-566): the extract_pores centroid at the basin peak, radius = sdf(peak)
+__device__ __forceinline__ pnm_pore centroid_pore(const float* __restrict__ sdf, Dims d, int ix,
+                                                  int iy, int iz, const float* o, const float* s,
+                                                  float radius) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  float sw = 0.0f, px = 0.0f, py = 0.0f, pz = 0.0f;
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const long long u = ((long long)wrap1(iz + dz, nz) * ny + wrap1(iy + dy, ny)) * nx +
+                            wrap1(ix + dx, nx);
+        const float v = sdf[u];
+        float w = v > 0.0f ? v : 0.0f;
+        w = __fmul_rn(w, w);
+        sw = __fadd_rn(sw, w);
+        px = __fadd_rn(px, __fmul_rn((float)dx, w));
+        py = __fadd_rn(py, __fmul_rn((float)dy, w));
+        pz = __fadd_rn(pz, __fmul_rn((float)dz, w));
+      }
+  float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+  if (sw > 1e-6f) {
+    fx = __fdiv_rn(px, sw);
+    fy = __fdiv_rn(py, sw);
+    fz = __fdiv_rn(pz, sw);
+  }
+  pnm_pore p;
+  p.x = __fadd_rn(o[0], __fmul_rn(__fadd_rn((float)ix, fx), s[0]));
+  p.y = __fadd_rn(o[1], __fmul_rn(__fadd_rn((float)iy, fy), s[1]));
+  p.z = __fadd_rn(o[2], __fmul_rn(__fadd_rn((float)iz, fz), s[2]));
+  p.radius = radius;
+  return p;
+}
+
+struct Geo {
+  float o[3], s[3];
+};
+
+// centres and trilinear periodic pore pressures (:534-613). g = (x - o)/s is evaluated in float
+// and widened, exactly as the reference's float Pore members and float origin/spacing.
+__global__ void k_centers_pressure(const float* __restrict__ sdf, Dims d, Geo g,
+                                   const int* __restrict__ peak, int np,
+                                   const double* __restrict__ p, pnm_pore* __restrict__ pores,
+                                   double* __restrict__ ppres) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < np; k += gridDim.x * blockDim.x) {
+    const int ci = peak[k];
+    const int3 c = coords_of(ci, nx, ny);
+    const pnm_pore po = centroid_pore(sdf, d, c.x, c.y, c.z, g.o, g.s, sdf[ci]);
+    pores[k] = po;
+    const double gg[3] = {(double)__fdiv_rn(__fsub_rn(po.x, g.o[0]), g.s[0]),
+                          (double)__fdiv_rn(__fsub_rn(po.y, g.o[1]), g.s[1]),
+                          (double)__fdiv_rn(__fsub_rn(po.z, g.o[2]), g.s[2])};
+    int b[3];
+    double f[3];
+    for (int a = 0; a < 3; ++a) {
+      const double fl = floor(gg[a]);
+      b[a] = (int)fl;
+      f[a] = __dsub_rn(gg[a], fl);
+    }
+    double acc = 0.0;
+    for (int dz = 0; dz < 2; ++dz)
+      for (int dy = 0; dy < 2; ++dy)
+        for (int dx = 0; dx < 2; ++dx) {
+          const double wx = dx ? f[0] : __dsub_rn(1.0, f[0]);
+          const double wy = dy ? f[1] : __dsub_rn(1.0, f[1]);
+          const double wz = dz ? f[2] : __dsub_rn(1.0, f[2]);
+          const double wt = __dmul_rn(__dmul_rn(wx, wy), wz);
+          const long long u = ((long long)pmod(b[2] + dz, nz) * ny + pmod(b[1] + dy, ny)) * nx +
+                              pmod(b[0] + dx, nx);
+          acc = __dadd_rn(acc, __dmul_rn(wt, p[u]));
+        }
+    ppres[k] = acc;
+  }
+}
+
+// flow basins (:621-652): flowLab = seg at the <=512-step ascent root of EVERY cell. Pore voxels
+// already carry their root in key[]; other cells chase the ascent pointers.
+__global__ void __launch_bounds__(256)
+    k_flow_basins(Dims d, const uint8_t* __restrict__ code, const int* __restrict__ key,
+                  const int* __restrict__ seg, int* __restrict__ flowLab) {
+  const long long n = d.n();
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (long long)gridDim.x * blockDim.x) {
+    const uint8_t c0 = code[v];
+    int root;
+    if (code_cls(c0) == CLS_PORE) {
+      root = key[v];
+    } else {
+      int3 q = coords_of(v, nx, ny);
+      int cur = (int)v;
+      for (int s = 0; s < 512; ++s) {
+        const int dir = code_dir(__ldg(&code[cur]));
+        if (dir == kSelf) break;
+        q.x = wrap1(q.x + (dir % 3) - 1, nx);
+        q.y = wrap1(q.y + ((dir / 3) % 3) - 1, ny);
+        q.z = wrap1(q.z + (dir / 9) - 1, nz);
+        cur = (q.z * ny + q.y) * nx + q.x;
+      }
+      root = cur;
+    }
+    flowLab[v] = __ldg(&seg[root]);
+  }
+}
+
+struct FieldPtrs {
+  const double *u, *v, *w, *ox, *oy, *oz;
+};
+__device__ __forceinline__ double openness(const FieldPtrs& f, int dd, long long nb) {
+  if (!f.ox) return 1.0;
+  return dd == 0 ? f.ox[nb] : (dd == 1 ? f.oy[nb] : f.oz[nb]);
+}
+__device__ __forceinline__ double velocity(const FieldPtrs& f, int dd, long long nb) {
+  return dd == 0 ? f.u[nb] : (dd == 1 ? f.v[nb] : f.w[nb]);
+}
+
+// face classification (:681-696): face fid = 3*cell + d is the +d face of the cell; interface if
+// the flow labels differ, both are pores (> 0) and the openness (of the +d neighbour's -d face)
+// is > 0; core if both cell centres are fluid (sdf > 0). Writes the interface and core bitmaps
+// over fids (a warp's 32 cells own exactly three 32-bit words) and the bounds of |q| and |o*A|
+// over the differing faces, which fix the fixed-point scales.
+__global__ void __launch_bounds__(256)
+    k_face_class(Dims d, const uint8_t* __restrict__ code, const int* __restrict__ flowLab,
+                 FieldPtrs f, double A0, double A1, double A2, uint32_t* __restrict__ ifbits,
+                 uint32_t* __restrict__ corebits, unsigned long long* bounds) {
+  const long long n = d.n();
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const double area[3] = {A0, A1, A2};
+  double mq = 0.0, mw = 0.0;
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
+       base += (long long)gridDim.x * blockDim.x) {
+    const long long c = base + threadIdx.x;
+    unsigned ib = 0, cb = 0;
+    if (c < n) {
+      const int3 q = coords_of(c, nx, ny);
+      const int a = flowLab[c];
+      const bool cpore = code_cls(code[c]) == CLS_PORE;
+#pragma unroll
+      for (int dd = 0; dd < 3; ++dd) {
+        const long long nb = ((long long)(dd == 2 ? wrap1(q.z + 1, nz) : q.z) * ny +
+                              (dd == 1 ? wrap1(q.y + 1, ny) : q.y)) * nx +
+                             (dd == 0 ? wrap1(q.x + 1, nx) : q.x);
+        const int b = flowLab[nb];
+        if (a == b) continue;
+        const double opn = openness(f, dd, nb);
+        const double qv = __dmul_rn(__dmul_rn(opn, velocity(f, dd, nb)), area[dd]);
+        mq = fmax(mq, fabs(qv));
+        if (a > 0 && b > 0 && opn > 0.0) {
+          ib |= 1u << dd;
+          mw = fmax(mw, fabs(__dmul_rn(opn, area[dd])));
+          if (cpore && code_cls(code[nb]) == CLS_PORE) cb |= 1u << dd;
+        }
+      }
+    }
+    const unsigned l = lane_id();
+    const long long wbase = (base + (threadIdx.x & ~31u)) * 3 / 32;  // first word of this warp
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int bit = 32 * j + (int)l;  // face index within the warp's 96 faces
+      const int src = bit / 3, dd = bit % 3;
+      const unsigned ibs = __shfl_sync(0xffffffffu, ib, src);
+      const unsigned cbs = __shfl_sync(0xffffffffu, cb, src);
+      const unsigned wi = __ballot_sync(0xffffffffu, (ibs >> dd) & 1u);
+      const unsigned wc = __ballot_sync(0xffffffffu, (cbs >> dd) & 1u);
+      if (l == 0 && (wbase + j) * 32 < 3 * n) {
+        ifbits[wbase + j] = wi;
+        corebits[wbase + j] = wc;
+      }
+    }
+  }
+  mq = warp_max(mq);
+  mw = warp_max(mw);
+  if (lane_id() == 0) {
+    atomic_max_abs(&bounds[0], mq);
+    atomic_max_abs(&bounds[1], mw);
+  }
+}
+
+// compaction of the interface faces (fid order) with their pair keys (lo << 32 | hi)
+__global__ void k_face_compact(Dims d, const uint32_t* __restrict__ ifbits,
+                               const unsigned* __restrict__ ifpref, long long words,
+                               const int* __restrict__ flowLab, int* __restrict__ fid,
+                               unsigned long long* __restrict__ fpair, int* __restrict__ par) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < words;
+       w += (long long)gridDim.x * blockDim.x) {
+    uint32_t b = ifbits[w];
+    unsigned k = ifpref[w];
+    while (b) {
+      const int j = __ffs(b) - 1;
+      b &= b - 1;
+      const long long fl = w * 32 + j;
+      const long long c = fl / 3;
+      const int dd = (int)(fl % 3);
+      const int3 q = coords_of(c, nx, ny);
+      const long long nb = ((long long)(dd == 2 ? wrap1(q.z + 1, nz) : q.z) * ny +
+                            (dd == 1 ? wrap1(q.y + 1, ny) : q.y)) * nx +
+                           (dd == 0 ? wrap1(q.x + 1, nx) : q.x);
+      const int a = flowLab[c], bb = flowLab[nb];
+      const int lo = a < bb ? a : bb, hi = a < bb ? bb : a;
+      fid[k] = (int)fl;
+      fpair[k] = ((unsigned long long)(unsigned)lo << 32) | (unsigned)hi;
+      par[k] = (int)k;
+      ++k;
+    }
+  }
+}
+
+struct FaceIndex {
+  const uint32_t* ifbits;
+  const unsigned* ifpref;
+  const uint32_t* corebits;
+  const unsigned long long* fpair;
+};
+
+// Visits every interface face of the same pair adjacent to face (c, dd) under the reference's
+// doubled-offset rule |2*dc + e_d2 - e_d|^2 <= 8 over the 27 wrapped neighbour cells
+// (:711-723, :776-791), calling fn(k2, is_core).
+template <class Fn>
+__device__ __forceinline__ void for_adjacent_faces(Dims d, const FaceIndex& fx, long long f,
+                                                   unsigned long long pk, Fn fn) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const long long c = f / 3;
+  const int dd = (int)(f % 3);
+  const int3 q = coords_of(c, nx, ny);
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const long long c2 =
+            ((long long)wrap1(q.z + dz, nz) * ny + wrap1(q.y + dy, ny)) * nx + wrap1(q.x + dx, nx);
+        for (int d2 = 0; d2 < 3; ++d2) {
+          const long long f2 = 3 * c2 + d2;
+          if (f2 == f) continue;
+          const int Dx = 2 * dx + (d2 == 0) - (dd == 0);
+          const int Dy = 2 * dy + (d2 == 1) - (dd == 1);
+          const int Dz = 2 * dz + (d2 == 2) - (dd == 2);
+          if (Dx * Dx + Dy * Dy + Dz * Dz > 8) continue;
+          if (!bitmap_test(fx.ifbits, f2)) continue;
+          const unsigned k2 = bitmap_rank(fx.ifbits, fx.ifpref, f2);
+          if (fx.fpair[k2] != pk) continue;
+          fn(k2, bitmap_test(fx.corebits, f2));
+        }
+      }
+}
+
+// Tier unions: core faces with adjacent core faces (core CCL, :699-756) and film faces with
+// adjacent film faces (the film components; :763-818). Roots are the minimum compact index,
+// which is the minimum fid since compaction preserves fid order.
+__global__ void __launch_bounds__(256)
+    k_face_unite(Dims d, FaceIndex fx, const int* __restrict__ fid, long long M, int* par,
+                 unsigned* err) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < M;
+       k += (long long)gridDim.x * blockDim.x) {
+    const long long f = fid[k];
+    const bool core = bitmap_test(fx.corebits, f);
+    const unsigned long long pk = fx.fpair[k];
+    for_adjacent_faces(d, fx, f, pk, [&](unsigned k2, bool core2) {
+      if (core2 == core && (long long)k2 > k) uf_unite(par, (int)k, (int)k2, err);
+    });
+  }
+}
+
+__global__ void k_face_flatten(long long M, int* par, unsigned* err) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < M;
+       k += (long long)gridDim.x * blockDim.x)
+    par[k] = uf_find(par, (int)k, err);
+}
+
+// Film attachment: a film component takes the smallest core-patch root adjacent to any of its
+// faces — the fixpoint of the reference's min propagation through films (:763-805). Components
+// adjacent to no core keep their own minimum (the leftover tier, :807-818).
+__global__ void __launch_bounds__(256)
+    k_film_attach(Dims d, FaceIndex fx, const int* __restrict__ fid, long long M,
+                  const int* __restrict__ par, int* __restrict__ minCore) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < M;
+       k += (long long)gridDim.x * blockDim.x) {
+    const long long f = fid[k];
+    if (bitmap_test(fx.corebits, f)) continue;
+    const unsigned long long pk = fx.fpair[k];
+    const int myroot = par[k];
+    for_adjacent_faces(d, fx, f, pk, [&](unsigned k2, bool core2) {
+      if (core2) atomicMin(&minCore[myroot], par[k2]);
+    });
+  }
+}
+
+__global__ void k_face_label(long long M, const FaceIndex fx, const int* __restrict__ fid,
+                             const int* __restrict__ par, const int* __restrict__ minCore,
+                             int* __restrict__ label, unsigned* __restrict__ isroot) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < M;
+       k += (long long)gridDim.x * blockDim.x) {
+    const int r = par[k];
+    int l = r;
+    if (!bitmap_test(fx.corebits, fid[k]) && minCore[r] != INT_MAX) l = minCore[r];
+    label[k] = l;
+    isroot[k] = (l == (int)k) ? 1u : 0u;
+  }
+}
+
+struct IsRoot {
+  const unsigned* f;
+  __device__ unsigned operator()(long long i) const { return f[i]; }
+};
+
+__global__ void k_root_keys(long long M, const unsigned* __restrict__ isroot,
+                            const unsigned* __restrict__ rpos,
+                            const unsigned long long* __restrict__ fpair, int b,
+                            uint64_t* __restrict__ keys, unsigned* __restrict__ vals) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < M;
+       k += (long long)gridDim.x * blockDim.x) {
+    if (!isroot[k]) continue;
+    const unsigned long long pk = fpair[k];
+    const unsigned lo = (unsigned)(pk >> 32), hi = (unsigned)(pk & 0xffffffffu);
+    const unsigned t = rpos[k];
+    keys[t] = ((uint64_t)(lo - 1u) << b) | (uint64_t)(hi - 1u);
+    vals[t] = (unsigned)k;
+  }
+}
+
+// throat slots in (pair, root fid) order (:820-862)
+__global__ void k_slots(long long nt, const uint64_t* __restrict__ keys,
+                        const unsigned* __restrict__ vals, int b, int* __restrict__ slotOf,
+                        int* __restrict__ throats) {
+  const uint64_t lowmask = (1ull << b) - 1ull;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nt;
+       t += (long long)gridDim.x * blockDim.x) {
+    slotOf[vals[t]] = (int)t;
+    throats[2 * t] = (int)(keys[t] >> b) + 1;
+    throats[2 * t + 1] = (int)(keys[t] & lowmask) + 1;
+  }
+}
+
+struct FluxParams {
+  double area[3];
+  double L[3];
+  float o[3], s[3];
+  int sq, sa, sc;  // fixed-point scales: fluxes/residuals, areas, centroid moments
+};
+
+// throat_flux (:883-942): for every +d face whose flow labels differ, q = o*vel*A on the +d
+// neighbour's -d face; resid[a-1] += q, resid[b-1] -= q; faces of a patch add +-q, o*A and the
+// area-weighted centroid moment (min-imaged against the lower pore's peak voxel) to their throat.
+__global__ void __launch_bounds__(256)
+    k_flux(Dims d, const int* __restrict__ flowLab, FieldPtrs f, FaceIndex fx,
+           const int* __restrict__ label, const int* __restrict__ slotOf,
+           const int* __restrict__ peak, FluxParams P, unsigned long long* accR,
+           unsigned long long* accQ, unsigned long long* accA, unsigned long long* accCx,
+           unsigned long long* accCy, unsigned long long* accCz) {
+  const long long n = d.n();
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
+       base += (long long)gridDim.x * blockDim.x) {
+    const long long c = base + threadIdx.x;
+    const bool valid = c < n;
+    int3 q = make_int3(0, 0, 0);
+    int a = 0;
+    if (valid) {
+      q = coords_of(c, nx, ny);
+      a = flowLab[c];
+    }
+#pragma unroll 1
+    for (int dd = 0; dd < 3; ++dd) {
+      int ta = -1, tb = -1, ts = -1;
+      I128 vq{0ull, 0ll}, vnq{0ull, 0ll}, vQ{0ull, 0ll}, vA{0ull, 0ll}, vC[3];
+      vC[0] = vC[1] = vC[2] = I128{0ull, 0ll};
+      if (valid) {
+        const long long nb = ((long long)(dd == 2 ? wrap1(q.z + 1, nz) : q.z) * ny +
+                              (dd == 1 ? wrap1(q.y + 1, ny) : q.y)) * nx +
+                             (dd == 0 ? wrap1(q.x + 1, nx) : q.x);
+        const int b = flowLab[nb];
+        if (a != b) {
+          const double opn = openness(f, dd, nb);
+          const double area = P.area[dd];
+          const double qv = __dmul_rn(__dmul_rn(opn, velocity(f, dd, nb)), area);
+          if (a > 0) {
+            ta = a - 1;
+            vq = to_fixed(qv, P.sq);
+          }
+          if (b > 0) {
+            tb = b - 1;
+            vnq = to_fixed(-qv, P.sq);
+          }
+          const long long fl = 3 * c + dd;
+          if (bitmap_test(fx.ifbits, fl)) {
+            const unsigned k = bitmap_rank(fx.ifbits, fx.ifpref, fl);
+            ts = slotOf[label[k]];
+            const int lo = a < b ? a : b;
+            const double w0 = __dmul_rn(opn, area);
+            vQ = to_fixed(a < b ? qv : -qv, P.sq);
+            vA = to_fixed(w0, P.sa);
+            const int pk = peak[lo - 1];
+            const int3 pc = coords_of(pk, nx, ny);
+            const int ci[3] = {q.x, q.y, q.z};
+            const int pi[3] = {pc.x, pc.y, pc.z};
+#pragma unroll
+            for (int a2 = 0; a2 < 3; ++a2) {
+              const double sp = (double)P.s[a2];
+              const double fpv = __dadd_rn((double)P.o[a2],
+                                           __dmul_rn(__dadd_rn((double)ci[a2], dd == a2 ? 0.5 : 0.0), sp));
+              const double pcv = __dadd_rn((double)P.o[a2], __dmul_rn((double)pi[a2], sp));
+              double dv = __dsub_rn(fpv, pcv);
+              dv = __dsub_rn(dv, __dmul_rn(P.L[a2], round(__ddiv_rn(dv, P.L[a2]))));
+              vC[a2] = to_fixed(__dmul_rn(w0, dv), P.sc);
+            }
+          }
+        }
+      }
+      warp_accumulate(accR, ta, vq);
+      warp_accumulate(accR, tb, vnq);
+      warp_accumulate(accQ, ts, vQ);
+      warp_accumulate(accA, ts, vA);
+      warp_accumulate(accCx, ts, vC[0]);
+      warp_accumulate(accCy, ts, vC[1]);
+      warp_accumulate(accCz, ts, vC[2]);
+    }
+  }
+}
+
+__global__ void k_fixed_to_double(const unsigned long long* __restrict__ acc, long long count,
+                                  int scale, double* __restrict__ out) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = from_fixed(acc[2 * i], (long long)acc[2 * i + 1], scale);
+}
+
+struct DpParams {
+  float o[3], s[3];
+  int N[3];
+  double L[3];
+  double g[3];
+};
+// throat_dp (:962-995): two-leg min-image image count from snapped integers, then
+// dp = (p_i - p_j) - sum_a g_a ((x_j - x_i) - L_a k_a); no contraction.
+__global__ void k_throat_dp(long long nt, const int* __restrict__ throats,
+                            const pnm_pore* __restrict__ pores, const double* __restrict__ ppres,
+                            const int* __restrict__ peak, const double* __restrict__ A,
+                            const double* __restrict__ Cx, const double* __restrict__ Cy,
+                            const double* __restrict__ Cz, DpParams P, double* __restrict__ dp) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nt;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int li = throats[2 * t], lj = throats[2 * t + 1];
+    const pnm_pore pi = pores[li - 1], pj = pores[lj - 1];
+    const double aw = A[t];
+    const int pk = peak[li - 1], pkj = peak[lj - 1];
+    const int ci[3] = {pk % P.N[0], (pk / P.N[0]) % P.N[1], pk / (P.N[0] * P.N[1])};
+    const int cj[3] = {pkj % P.N[0], (pkj / P.N[0]) % P.N[1], pkj / (P.N[0] * P.N[1])};
+    const double pip[3] = {(double)pi.x, (double)pi.y, (double)pi.z};
+    const double pjp[3] = {(double)pj.x, (double)pj.y, (double)pj.z};
+    const double C[3] = {Cx[t], Cy[t], Cz[t]};
+    double macro = 0.0;
+    for (int a = 0; a < 3; ++a) {
+      const double sp = (double)P.s[a];
+      const double anc = __dadd_rn((double)P.o[a], __dmul_rn((double)ci[a], sp));
+      const double ancj = __dadd_rn((double)P.o[a], __dmul_rn((double)cj[a], sp));
+      const double ct = __ddiv_rn(C[a], aw);
+      const long long Dc =
+          llround(__ddiv_rn(__dsub_rn(ancj, anc), sp)) - llround(__dadd_rn(__ddiv_rn(ct, sp), 1e-6));
+      const long long k = llround(__ddiv_rn((double)Dc, (double)P.N[a]));
+      const double leg = __dsub_rn(__dsub_rn(pjp[a], pip[a]), __dmul_rn(P.L[a], (double)k));
+      macro = __dadd_rn(macro, __dmul_rn(P.g[a], leg));
+    }
+    dp[t] = __dsub_rn(__dsub_rn(ppres[li - 1], ppres[lj - 1]), macro);
+  }
+}
+
+__global__ void k_fill_int(int* p, long long m, int v) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (long long)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+inline unsigned gridn(long long work, int sm_count, int per_sm = 8) {
+  long long b = (work + 255) / 256;
+  const long long cap = (long long)sm_count * per_sm;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+// scale so that 2^31 terms of magnitude <= bound sum below 2^125 (headroom in a signed 128-bit)
+inline int fixed_scale(double bound) {
+  if (!(bound > 0.0) || !std::isfinite(bound)) return 0;
+  int e;
+  std::frexp(bound, &e);  // bound < 2^e
+  return 125 - 31 - e;
+}
+
+}  // namespace
+
+Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const float spacing[3],
+                        const FlowInputs& in, FlowOutputsHost* out) {
+  cudaStream_t s = c.stream;
+  const Dims d = st.d;
+  const long long n = d.n();
+  const int np = st.n_pore_labels;
+  *out = FlowOutputsHost{};
+  if (np <= 0) return Status::ok();  // no pore label: empty network (:523-524)
+
+  // seg (labels) for the flow-basin lookup
+  int32_t* seg = nullptr;
+  PNM_TRY(c.buf(S_SEG, n, &seg));
+  {
+    int32_t* dummy = nullptr;
+    int64_t m = 0;
+    PNM_TRY(run_seg_and_topology(c, st, seg, false, &dummy, &m));
+  }
+
+  int *peak, *flowLab;
+  pnm_pore* pores;
+  double* ppres;
+  PNM_TRY(c.buf(S_PEAK, np, &peak));
+  PNM_TRY(c.buf(S_FLOWLAB, n, &flowLab));
+  PNM_TRY(c.buf(S_NPORES_OUT, np, &pores));
+  PNM_TRY(c.buf(S_PPRES, np, &ppres));
+  PNM_CUDA(cudaMemsetAsync(peak, 0, np * sizeof(int), s));
+  const long long words = (n + 31) / 32;
+  k_peaks<<<gridn(words, c.sm_count), 256, 0, s>>>(st.peakbits, words, st.code, seg, peak);
+  Geo geo;
+  for (int a = 0; a < 3; ++a) {
+    geo.o[a] = origin[a];
+    geo.s[a] = spacing[a];
+  }
+  k_centers_pressure<<<gridn(np, c.sm_count), 256, 0, s>>>(st.sdf, d, geo, peak, np, in.p, pores,
+                                                           ppres);
+  k_flow_basins<<<gridn(n, c.sm_count), 256, 0, s>>>(d, st.code, st.key, seg, flowLab);
+  PNM_CUDA(cudaGetLastError());
+
+  // face classification + bounds
+  const long long nf = 3 * n;
+  const long long fwords = (nf + 31) / 32;
+  uint32_t *ifbits, *corebits;
+  unsigned *ifpref, *scan0;
+  unsigned long long* bounds;
+  PNM_TRY(c.buf(S_FBITS, fwords + 1, &ifbits));
+  PNM_TRY(c.buf(S_FCORE, fwords + 1, &corebits));
+  PNM_TRY(c.buf(S_FPREF, fwords + 1, &ifpref));
+  PNM_TRY(c.buf(S_SCAN0, nf / SCAN_TILE + 2, &scan0));  // bounds every scan below (m <= 3n)
+  PNM_TRY(c.buf(S_ACC, 4, &bounds));
+  PNM_CUDA(cudaMemsetAsync(bounds, 0, 4 * sizeof(unsigned long long), s));
+  const double Ax = (double)spacing[1] * spacing[2], Ay = (double)spacing[0] * spacing[2],
+               Az = (double)spacing[0] * spacing[1];  // :869-870
+  const FieldPtrs fp{in.u, in.v, in.w, in.ox, in.oy, in.oz};
+  k_face_class<<<gridn(n, c.sm_count), 256, 0, s>>>(d, st.code, flowLab, fp, Ax, Ay, Az, ifbits,
+                                                     corebits, bounds);
+  exclusive_scan(PopcountOf{ifbits}, fwords, ifpref, scan0, s);
+  PNM_CUDA(cudaGetLastError());
+  unsigned M32 = 0;
+  unsigned long long hb[2];
+  PNM_CUDA(cudaMemcpyAsync(&M32, ifpref + fwords, 4, cudaMemcpyDeviceToHost, s));
+  PNM_CUDA(cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, s));
+  PNM_CUDA(cudaStreamSynchronize(s));
+  const long long M = M32;
+  double bq, bw;
+  std::memcpy(&bq, &hb[0], 8);
+  std::memcpy(&bw, &hb[1], 8);
+
+  // compaction + two-tier face CCL
+  int *fid, *par, *minCore, *label, *slotOf, *throats_d;
+  unsigned long long* fpair;
+  unsigned *isroot, *rpos;
+  const long long Mx = std::max<long long>(M, 1);
+  PNM_TRY(c.buf(S_FID, Mx, &fid));
+  PNM_TRY(c.buf(S_FPAIR, Mx, &fpair));
+  PNM_TRY(c.buf(S_FPAR, Mx, &par));
+  PNM_TRY(c.buf(S_FMINCORE, Mx, &minCore));
+  PNM_TRY(c.buf(S_FLABEL, Mx, &label));
+  PNM_TRY(c.buf(S_ROOTFLAG, Mx, &isroot));
+  PNM_TRY(c.buf(S_TDP, Mx + 1, &rpos));
+  PNM_TRY(c.buf(S_SLOTOF, Mx, &slotOf));
+  PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_ERR], 0, sizeof(unsigned), s));
+  long long nt = 0;
+  const FaceIndex fx{ifbits, ifpref, corebits, fpair};
+  int b = 1;
+  while ((1ll << b) < (long long)np) ++b;  // pore labels 1..np -> (label-1) in b bits
+  if (M > 0) {
+    k_face_compact<<<gridn(fwords, c.sm_count), 256, 0, s>>>(d, ifbits, ifpref, fwords, flowLab,
+                                                             fid, fpair, par);
+    k_face_unite<<<gridn(M, c.sm_count), 256, 0, s>>>(d, fx, fid, M, par, &c.d_cnt[CNT_ERR]);
+    k_face_flatten<<<gridn(M, c.sm_count), 256, 0, s>>>(M, par, &c.d_cnt[CNT_ERR]);
+    k_fill_int<<<gridn(M, c.sm_count), 256, 0, s>>>(minCore, M, INT_MAX);
+    k_film_attach<<<gridn(M, c.sm_count), 256, 0, s>>>(d, fx, fid, M, par, minCore);
+    k_face_label<<<gridn(M, c.sm_count), 256, 0, s>>>(M, fx, fid, par, minCore, label, isroot);
+    exclusive_scan(IsRoot{isroot}, M, rpos, scan0, s);
+    PNM_CUDA(cudaGetLastError());
+    unsigned nt32 = 0;
+    PNM_CUDA(cudaMemcpyAsync(&nt32, rpos + M, 4, cudaMemcpyDeviceToHost, s));
+    PNM_TRY(c.read_counters());
+    if (c.h_cnt[CNT_ERR] & ERRF_UF_LIMIT)
+      return Status{PNM_ERR_NOT_CONVERGED, "face union-find exceeded its iteration limit"};
+    nt = nt32;
+  }
+
+  // throat order (pair, root fid): roots are listed in fid order; a stable sort by pair keeps it
+  PNM_TRY(c.buf(S_THROATS, 2 * std::max<long long>(nt, 1), &throats_d));
+  if (nt > 0) {
+    uint64_t *ka, *kb;
+    unsigned *va, *vb, *hist, *stmp;
+    PNM_TRY(c.buf(S_KEYS_A, nt, &ka));
+    PNM_TRY(c.buf(S_KEYS_B, nt, &kb));
+    PNM_TRY(c.buf(S_VALS_A, nt, &va));
+    PNM_TRY(c.buf(S_VALS_B, nt, &vb));
+    PNM_TRY(c.buf(S_RSHIST, 256 * (nt / RS_TILE + 1) + 1, &hist));
+    PNM_TRY(c.buf(S_SCAN1, (256 * (nt / RS_TILE + 1)) / SCAN_TILE + 2, &stmp));
+    k_root_keys<<<gridn(M, c.sm_count), 256, 0, s>>>(M, isroot, rpos, fpair, b, ka, va);
+    const bool in_b = radix_sort(ka, va, kb, vb, nt, 0, 2 * b, hist, stmp, s);
+    k_slots<<<gridn(nt, c.sm_count), 256, 0, s>>>(nt, in_b ? kb : ka, in_b ? vb : va, b, slotOf,
+                                                  throats_d);
+    PNM_CUDA(cudaGetLastError());
+  }
+
+  // fluxes: exact fixed-point sums
+  FluxParams P;
+  P.area[0] = Ax;
+  P.area[1] = Ay;
+  P.area[2] = Az;
+  const int N[3] = {d.nx, d.ny, d.nz};
+  double Lmax = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    P.L[a] = (double)N[a] * spacing[a];  // :876
+    P.o[a] = origin[a];
+    P.s[a] = spacing[a];
+    Lmax = std::max(Lmax, P.L[a]);
+  }
+  P.sq = fixed_scale(bq);
+  P.sa = fixed_scale(bw);
+  P.sc = fixed_scale(bw * (Lmax + 1.0));
+  const long long nacc = (long long)np + 5 * std::max<long long>(nt, 1);
+  unsigned long long* acc;
+  PNM_TRY(c.buf(S_REC, 2 * nacc, &acc));
+  PNM_CUDA(cudaMemsetAsync(acc, 0, 2 * nacc * sizeof(unsigned long long), s));
+  unsigned long long* accR = acc;
+  unsigned long long* accQ = accR + 2 * (long long)np;
+  const long long ntx = std::max<long long>(nt, 1);
+  unsigned long long* accA = accQ + 2 * ntx;
+  unsigned long long* accCx = accA + 2 * ntx;
+  unsigned long long* accCy = accCx + 2 * ntx;
+  unsigned long long* accCz = accCy + 2 * ntx;
+  k_flux<<<gridn(n, c.sm_count), 256, 0, s>>>(d, flowLab, fp, fx, label, slotOf, peak, P, accR,
+                                               accQ, accA, accCx, accCy, accCz);
+  double* dres;
+  PNM_TRY(c.buf(S_FLOWOUT, nacc + ntx, &dres));
+  double* resid = dres;
+  double* Q = resid + np;
+  double* A = Q + ntx;
+  double* Cx = A + ntx;
+  double* Cy = Cx + ntx;
+  double* Cz = Cy + ntx;
+  double* dp = Cz + ntx;
+  k_fixed_to_double<<<gridn(np, c.sm_count), 256, 0, s>>>(accR, np, P.sq, resid);
+  if (nt > 0) {
+    k_fixed_to_double<<<gridn(nt, c.sm_count), 256, 0, s>>>(accQ, nt, P.sq, Q);
+    k_fixed_to_double<<<gridn(nt, c.sm_count), 256, 0, s>>>(accA, nt, P.sa, A);
+    k_fixed_to_double<<<gridn(nt, c.sm_count), 256, 0, s>>>(accCx, nt, P.sc, Cx);
+    k_fixed_to_double<<<gridn(nt, c.sm_count), 256, 0, s>>>(accCy, nt, P.sc, Cy);
+    k_fixed_to_double<<<gridn(nt, c.sm_count), 256, 0, s>>>(accCz, nt, P.sc, Cz);
+    DpParams D;
+    for (int a = 0; a < 3; ++a) {
+      D.o[a] = origin[a];
+      D.s[a] = spacing[a];
+      D.N[a] = N[a];
+      D.L[a] = P.L[a];
+      D.g[a] = in.grad_p[a];
+    }
+    k_throat_dp<<<gridn(nt, c.sm_count), 256, 0, s>>>(nt, throats_d, pores, ppres, peak, A, Cx,
+                                                      Cy, Cz, D, dp);
+  }
+  PNM_CUDA(cudaGetLastError());
+
+  out->pores.resize(np);
+  out->pore_pressure.resize(np);
+  out->pore_residual.resize(np);
+  out->throats.resize(2 * nt);
+  out->throat_flow.resize(nt);
+  out->throat_area.resize(nt);
+  out->throat_dp.resize(nt);
+  PNM_CUDA(cudaMemcpyAsync(out->pores.data(), pores, np * sizeof(pnm_pore), cudaMemcpyDeviceToHost, s));
+  PNM_CUDA(cudaMemcpyAsync(out->pore_pressure.data(), ppres, np * 8, cudaMemcpyDeviceToHost, s));
+  PNM_CUDA(cudaMemcpyAsync(out->pore_residual.data(), resid, np * 8, cudaMemcpyDeviceToHost, s));
+  if (nt > 0) {
+    PNM_CUDA(cudaMemcpyAsync(out->throats.data(), throats_d, 2 * nt * 4, cudaMemcpyDeviceToHost, s));
+    PNM_CUDA(cudaMemcpyAsync(out->throat_flow.data(), Q, nt * 8, cudaMemcpyDeviceToHost, s));
+    PNM_CUDA(cudaMemcpyAsync(out->throat_area.data(), A, nt * 8, cudaMemcpyDeviceToHost, s));
+    PNM_CUDA(cudaMemcpyAsync(out->throat_dp.data(), dp, nt * 8, cudaMemcpyDeviceToHost, s));
+  }
+  PNM_CUDA(cudaStreamSynchronize(s));
+  return Status::ok();
+}
+
+}  // namespace pnm

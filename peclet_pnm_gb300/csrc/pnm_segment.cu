@@ -1,0 +1,725 @@
+// Extraction kernels: SDF pass (pores, ascent pointers, classes, tile-local marker CCL),
+// cross-tile CCL merge, resolve (CCL roots, gradient roots, first flood sweep), BFS-layer flood,
+// first-appearance renumbering, fused seg write + topology pair emission, and pore compaction.
+//
+// Reference: src/pore_extraction.hpp (cited per kernel). The integer results are bit-exact with
+// it; float pore records are bit-exact because every float operation is an explicit
+// round-to-nearest intrinsic in the reference's order (and the library is built with
+// -fmad=false).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdint>
+#include <cstring>
+
+#include "pnm_ctx.h"
+#include "pnm_device.cuh"
+
+namespace pnm {
+
+constexpr int TX = 32, TY = 8, TZ = 8;  // SDF-pass tile: 2048 voxels, 256 threads
+constexpr int kBig = INT_MAX;           // unset min-index / non-marker parent
+
+// ---- 1. SDF pass ---------------------------------------------------------------------------
+// Per voxel, from a shared-memory tile with a one-voxel periodic halo:
+//  * ascent direction = lexicographic max of (sdf, wrapped index) over the voxel and its 26
+//    neighbours, scanned dz->dy->dx with the reference's comparisons (pore_extraction.hpp:284-304,
+//    :632-644); equal to "strict local max" when it points at the voxel itself (:93-104);
+//  * class (marker :177, flood :245-248, pore :276), flood seed (a marker neighbour);
+//  * peak bit for extract_pores (:89-106): !(sdf <= 0) and the voxel is its own ascent target;
+//  * tile-local union-find of the markers over the 13 forward neighbours (:204-222), written to
+//    L as the global id of the tile-local root. Non-markers get L = kBig.
+__global__ void __launch_bounds__(TX* TY)
+    k_sdf_pass(const float* __restrict__ sdf, Dims d, float thr, uint8_t* __restrict__ code,
+               int* __restrict__ L, uint32_t* __restrict__ peakbits) {
+  constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2, NT = TX * TY;
+  __shared__ float s[HZ][HY][HX];
+  __shared__ int lab[TZ * TY * TX];
+  __shared__ int wx[HX], wy[HY], wz[HZ];
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const long long nxy = (long long)nx * ny;
+  const int X0 = blockIdx.x * TX, Y0 = blockIdx.y * TY, Z0 = blockIdx.z * TZ;
+  const int t = threadIdx.x;
+  if (t < HX) wx[t] = ((X0 - 1 + t) % nx + nx) % nx;
+  if (t < HY) wy[t] = ((Y0 - 1 + t) % ny + ny) % ny;
+  if (t < HZ) wz[t] = ((Z0 - 1 + t) % nz + nz) % nz;
+  __syncthreads();
+  for (int i = t; i < HX * HY * HZ; i += NT) {
+    const int hx = i % HX, hy = (i / HX) % HY, hz = i / (HX * HY);
+    s[hz][hy][hx] = __ldg(&sdf[wz[hz] * nxy + (long long)wy[hy] * nx + wx[hx]]);
+  }
+  __syncthreads();
+  const int tx = t % TX, ty = t / TX;
+  const int gx = X0 + tx, gy = Y0 + ty;
+  const bool inxy = gx < nx && gy < ny;
+  for (int tz = 0; tz < TZ; ++tz) {
+    const int gz = Z0 + tz;
+    const int li = (tz * TY + ty) * TX + tx;
+    int lb = -1;
+    if (inxy && gz < nz) {
+      const long long ci = gz * nxy + (long long)gy * nx + gx;
+      const float cv = s[tz + 1][ty + 1][tx + 1];
+      float bv = cv;
+      long long best = ci;
+      int bdir = kSelf;
+      bool mk_nb = false;
+#pragma unroll
+      for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+          for (int dx = -1; dx <= 1; ++dx) {
+            const int k = (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1);
+            if (k == kSelf) continue;
+            const float nv = s[tz + 1 + dz][ty + 1 + dy][tx + 1 + dx];
+            const long long ni =
+                wz[tz + 1 + dz] * nxy + (long long)wy[ty + 1 + dy] * nx + wx[tx + 1 + dx];
+            if (nv > bv) {
+              bv = nv;
+              best = ni;
+              bdir = k;
+            } else if (nv == bv && ni > best) {
+              best = ni;
+              bdir = k;
+            }
+            mk_nb |= (nv < thr);
+          }
+      const int cls = cv > 0.0f ? CLS_PORE
+                                : (cv < thr ? CLS_MARKER : (!(cv >= 0.0f) ? CLS_FLOOD : CLS_ZERO));
+      code[ci] = make_code(bdir, cls, cls == CLS_FLOOD && mk_nb);
+      if (!(cv <= 0.0f) && bdir == kSelf) atomicOr(&peakbits[ci >> 5], 1u << (ci & 31));
+      if (cls == CLS_MARKER) lb = li;
+    }
+    lab[li] = lb;
+  }
+  __syncthreads();
+  // tile-local unions over the 13 forward neighbours that lie inside the tile and the volume
+  const int TXe = min(TX, nx - X0), TYe = min(TY, ny - Y0), TZe = min(TZ, nz - Z0);
+  for (int tz = 0; tz < TZ; ++tz) {
+    const int li = (tz * TY + ty) * TX + tx;
+    if (lab[li] == -1) continue;
+#pragma unroll
+    for (int k = 0; k < 13; ++k) {
+      const int dz = k < 9 ? 1 : 0;
+      const int dy = k < 9 ? (k / 3) - 1 : (k < 12 ? 1 : 0);
+      const int dx = k < 12 ? (k % 3) - 1 : 1;
+      const int lx = tx + dx, ly = ty + dy, lz = tz + dz;
+      if (lx < 0 || lx >= TXe || ly < 0 || ly >= TYe || lz >= TZe) continue;
+      const int lj = (lz * TY + ly) * TX + lx;
+      if (lab[lj] != -1) uf_unite_s(lab, li, lj);
+    }
+  }
+  __syncthreads();
+  for (int tz = 0; tz < TZ; ++tz) {
+    const int gz = Z0 + tz;
+    if (!inxy || gz >= nz) continue;
+    const int li = (tz * TY + ty) * TX + tx;
+    const long long ci = gz * nxy + (long long)gy * nx + gx;
+    int out = kBig;
+    if (lab[li] != -1) {
+      const int r = uf_find_s(lab, li);
+      const int rx = r % TX, ry = (r / TX) % TY, rz = r / (TX * TY);
+      out = (int)((Z0 + rz) * nxy + (long long)(Y0 + ry) * nx + (X0 + rx));
+    }
+    L[ci] = out;
+  }
+}
+
+// ---- 2. cross-tile CCL merge ------------------------------------------------------------------
+// Every marker voxel unites with those of its 13 forward periodic neighbours (the reference's
+// merge set, pore_extraction.hpp:204-206) that the tile-local pass did not see.
+__global__ void __launch_bounds__(TX* TY) k_ccl_boundary(Dims d, int* L, unsigned* err) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const long long nxy = (long long)nx * ny;
+  const int X0 = blockIdx.x * TX, Y0 = blockIdx.y * TY, Z0 = blockIdx.z * TZ;
+  const int TXe = min(TX, nx - X0), TYe = min(TY, ny - Y0), TZe = min(TZ, nz - Z0);
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  if (tx >= TXe || ty >= TYe) return;
+  const bool edge_xy = tx == 0 || tx == TXe - 1 || ty == 0 || ty == TYe - 1;
+  const int gx = X0 + tx, gy = Y0 + ty;
+  for (int tz = 0; tz < TZe; ++tz) {
+    if (!edge_xy && tz != TZe - 1) continue;
+    const int gz = Z0 + tz;
+    const int ci = (int)(gz * nxy + (long long)gy * nx + gx);
+    if (L[ci] == kBig) continue;
+#pragma unroll
+    for (int k = 0; k < 13; ++k) {
+      const int dz = k < 9 ? 1 : 0;
+      const int dy = k < 9 ? (k / 3) - 1 : (k < 12 ? 1 : 0);
+      const int dx = k < 12 ? (k % 3) - 1 : 1;
+      const int lx = tx + dx, ly = ty + dy, lz = tz + dz;
+      if (lx >= 0 && lx < TXe && ly >= 0 && ly < TYe && lz < TZe) continue;  // seen locally
+      const int ux = wrap1(gx + dx, nx), uy = wrap1(gy + dy, ny), uz = wrap1(gz + dz, nz);
+      const int u = (int)(uz * nxy + (long long)uy * nx + ux);
+      if (ld_relaxed(&L[u]) == kBig) continue;
+      uf_unite(L, ci, u, err);
+    }
+  }
+}
+
+// ---- 3. resolve ----------------------------------------------------------------------------------
+// Gradient root of a voxel: follow the ascent pointers for at most 512 moves
+// (pore_extraction.hpp:277-309 and :626-648; MAX_STEPS = 512).
+__device__ __forceinline__ int chase_root(const uint8_t* __restrict__ code, int v, Dims d) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+  int cur = v;
+  for (int s = 0; s < 512; ++s) {
+    const int dir = code_dir(__ldg(&code[cur]));
+    if (dir == kSelf) break;
+    x = wrap1(x + (dir % 3) - 1, nx);
+    y = wrap1(y + ((dir / 3) % 3) - 1, ny);
+    z = wrap1(z + (dir / 9) - 1, nz);
+    cur = (z * ny + y) * nx + x;
+  }
+  return cur;
+}
+
+// For every voxel: marker -> key ~root(CCL) and the root joins the key list; pore -> key =
+// gradient root, atomicMin of the voxel id into L[root] (first-appearance index; pore voxels'
+// L started at kBig) and, on first touch, the root joins the key list; flood seed -> label =
+// min CCL root over its marker neighbours (the first Jacobi sweep, :250-258), queued as the
+// first BFS layer; everything else -> KEY_NONE.
+__global__ void __launch_bounds__(256)
+    k_resolve(Dims d, const uint8_t* __restrict__ code, int* L, int* __restrict__ key,
+              int* __restrict__ keylist, int* __restrict__ front, unsigned* cnt) {
+  const long long n = d.n();
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  unsigned* err = &cnt[CNT_ERR];
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
+       base += (long long)gridDim.x * blockDim.x) {
+    const long long vl = base + threadIdx.x;
+    const bool valid = vl < n;
+    const int v = (int)vl;
+    int k = KEY_NONE, agg = -1;
+    bool new_key = false, seed = false;
+    if (valid) {
+      const uint8_t c = code[v];
+      const int cls = code_cls(c);
+      if (cls == CLS_MARKER) {
+        const int r = uf_find(L, v, err);
+        k = ~r;
+        new_key = (r == v);
+      } else if (cls == CLS_PORE) {
+        const int r = chase_root(code, v, d);
+        k = r;
+        agg = r;
+      } else if (cls == CLS_FLOOD && code_seed(c)) {
+        const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+        int best = INT_MAX;
+        for (int dz = -1; dz <= 1; ++dz)
+          for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+              if (!dx && !dy && !dz) continue;
+              const int u = (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx);
+              if (code_cls(__ldg(&code[u])) == CLS_MARKER) best = min(best, uf_find(L, u, err));
+            }
+        k = ~best;
+        seed = true;
+      }
+      key[v] = k;
+    }
+    // warp-aggregated first-appearance minimum for pore basins: lanes hold consecutive voxel
+    // ids, so the lowest lane of each same-root group carries the group minimum
+    const unsigned peers = __match_any_sync(0xffffffffu, agg);
+    if (agg >= 0 && (__ffs(peers) - 1) == (int)lane_id()) {
+      const int old = atomicMin(&L[agg], v);
+      if (old == kBig) new_key = true;
+    }
+    const int kpos = warp_append(&cnt[CNT_KEYS], new_key);
+    if (new_key) keylist[kpos] = (agg >= 0 ? agg : v);
+    const int fpos = warp_append(&cnt[CNT_FRONT0], seed);
+    if (seed) front[fpos] = v;
+  }
+}
+
+// ---- 4. BFS-layer flood (the reference's Jacobi sweeps, pore_extraction.hpp:237-269) ------------
+// Layer t = unlabelled flood voxels adjacent to layer t-1; a layer-t voxel takes the smallest
+// label among its neighbours labelled in layers < t. Discovery marks layer t PENDING, assignment
+// computes labels into `tmp` (indexed like the frontier), and the next discovery publishes them,
+// so no voxel ever sees a same-layer label — exactly the double-buffered sweep.
+__global__ void __launch_bounds__(256)
+    k_flood_discover(Dims d, const uint8_t* __restrict__ code, int* key, int* L,
+                     const int* __restrict__ fin, const unsigned* nin_p, const int* tmp,
+                     int publish, int* __restrict__ fout, unsigned* nout_p, unsigned* cnt) {
+  const unsigned nin = *nin_p;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nin;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int v = fin[i];
+    const int lab = publish ? tmp[i] : ~key[v];
+    if (publish) key[v] = ~lab;
+    atomicMin(&L[lab], v);  // first appearance of the solid label (roots start at L[r] == r)
+    const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          if (!dx && !dy && !dz) continue;
+          const int u = (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx);
+          if (code_cls(__ldg(&code[u])) != CLS_FLOOD) continue;
+          if (ld_relaxed(&key[u]) != KEY_NONE) continue;
+          if (atomicCAS(&key[u], KEY_NONE, KEY_PENDING) == KEY_NONE) {
+            const unsigned pos = atomicAdd(nout_p, 1u);
+            fout[pos] = u;
+          }
+        }
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_flood_assign(Dims d, const int* __restrict__ key, const int* __restrict__ f,
+                   const unsigned* n_p, int* __restrict__ tmp) {
+  const unsigned nf = *n_p;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nf;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int v = f[i];
+    const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+    int bestk = INT_MIN;  // largest solid key == smallest label
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          if (!dx && !dy && !dz) continue;
+          const int u = (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx);
+          const int k = key[u];
+          if (key_is_solid(k)) bestk = max(bestk, k);
+        }
+    tmp[i] = ~bestk;
+  }
+}
+
+// ---- 5. first-appearance renumbering (pore_extraction.hpp:319-382) --------------------------------
+// Label ids are ranks of each label's minimum voxel id: flag those minima in two bitmaps (pore /
+// solid), prefix-count the bitmaps, and write the signed id back into L[key].
+__global__ void k_key_first(const int* __restrict__ keylist, const unsigned* nkeys_p,
+                            const int* __restrict__ L, const uint8_t* __restrict__ code,
+                            uint32_t* firstP, uint32_t* firstS) {
+  const unsigned nk = *nkeys_p;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nk;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int k = keylist[i];
+    const int m = L[k];
+    uint32_t* bits = code_cls(code[k]) == CLS_PORE ? firstP : firstS;
+    atomicOr(&bits[m >> 5], 1u << (m & 31));
+  }
+}
+
+__global__ void k_key_id(const int* __restrict__ keylist, const unsigned* nkeys_p, int* L,
+                         const uint8_t* __restrict__ code, const uint32_t* firstP,
+                         const unsigned* prefP, const uint32_t* firstS, const unsigned* prefS) {
+  const unsigned nk = *nkeys_p;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nk;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int k = keylist[i];
+    const int m = L[k];
+    L[k] = code_cls(code[k]) == CLS_PORE ? (int)bitmap_rank(firstP, prefP, m) + 1
+                                         : -(int)bitmap_rank(firstS, prefS, m) - 1;
+  }
+}
+
+// ---- 6. seg write + topology pair emission (pore_extraction.hpp:378-381 and :414-431) -----------
+__device__ __forceinline__ int label_of_key(const int* __restrict__ L, int k) {
+  if (k >= 0) return __ldg(&L[k]);
+  if (key_is_solid(k)) return __ldg(&L[~k]);
+  return 0;
+}
+__device__ __forceinline__ uint64_t pair_key(int a, int b) {
+  const int lo = a < b ? a : b, hi = a < b ? b : a;
+  return ((uint64_t)((uint32_t)lo ^ 0x80000000u) << 32) | (uint64_t)((uint32_t)hi ^ 0x80000000u);
+}
+constexpr uint64_t kEmpty = ~0ull;  // no valid pair key is all ones (lo < hi)
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ull;
+  x ^= x >> 33;
+  return x;
+}
+constexpr int kMaxProbe = 4096;
+__device__ __forceinline__ void hash_insert(unsigned long long* table, uint64_t mask, uint64_t k,
+                                            unsigned* err, unsigned* count) {
+  uint64_t h = mix64(k) & mask;
+  for (int p = 0; p < kMaxProbe; ++p) {
+    const unsigned long long cur = *((volatile unsigned long long*)&table[h]);
+    if (cur == k) return;
+    if (cur == kEmpty) {
+      const unsigned long long old = atomicCAS(&table[h], kEmpty, (unsigned long long)k);
+      if (old == kEmpty) {
+        atomicAdd(count, 1u);
+        return;
+      }
+      if (old == k) return;
+    }
+    h = (h + 1) & mask;
+  }
+  atomicOr(err, ERRF_HASH_FULL);
+}
+
+struct KeyLabels {  // label of voxel v from key[] and the id table in L[]
+  const int* key;
+  const int* L;
+  __device__ int operator()(long long v) const { return label_of_key(L, __ldg(&key[v])); }
+};
+struct SegLabels {  // label of voxel v from a seg array
+  const int* seg;
+  __device__ int operator()(long long v) const { return __ldg(&seg[v]); }
+};
+
+// One pass: seg[v] (optional) and every differing (+x,+y,+z) periodic face pair into the hash set.
+// Identical pairs within a warp are merged before the global insert; lab_min/lab_max track the
+// label range for the sort.
+template <class Lab>
+__global__ void __launch_bounds__(256)
+    k_seg_topo(Dims d, Lab lab, int* __restrict__ seg, int want_pairs, unsigned long long* table,
+               uint64_t mask, unsigned* cnt, int* range) {
+  const long long n = d.n();
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  int lmin = INT_MAX, lmax = INT_MIN;
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
+       base += (long long)gridDim.x * blockDim.x) {
+    const long long v = base + threadIdx.x;
+    const bool valid = v < n;
+    int s0 = 0;
+    int x = 0, y = 0, z = 0;
+    if (valid) {
+      s0 = lab(v);
+      if (seg) seg[v] = s0;
+      x = (int)(v % nx);
+      y = (int)((v / nx) % ny);
+      z = (int)(v / ((long long)nx * ny));
+    }
+    if (!want_pairs) continue;
+#pragma unroll
+    for (int dd = 0; dd < 3; ++dd) {
+      uint64_t pk = kEmpty;
+      if (valid) {
+        const int ux = dd == 0 ? wrap1(x + 1, nx) : x;
+        const int uy = dd == 1 ? wrap1(y + 1, ny) : y;
+        const int uz = dd == 2 ? wrap1(z + 1, nz) : z;
+        const int s1 = lab(((long long)uz * ny + uy) * nx + ux);
+        if (s1 != s0) {
+          pk = pair_key(s0, s1);
+          lmin = min(lmin, min(s0, s1));
+          lmax = max(lmax, max(s0, s1));
+        }
+      }
+      const unsigned peers = __match_any_sync(0xffffffffu, pk);
+      if (pk != kEmpty && (__ffs(peers) - 1) == (int)lane_id())
+        hash_insert(table, mask, pk, &cnt[CNT_ERR], &cnt[CNT_FLOW_SPARE1]);
+    }
+  }
+  if (want_pairs) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      lmin = min(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
+      lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+    }
+    if (lane_id() == 0 && lmin <= lmax) {
+      atomicMin(&range[0], lmin);
+      atomicMax(&range[1], lmax);
+    }
+  }
+}
+
+struct Occupied {
+  const unsigned long long* t;
+  __device__ unsigned operator()(long long i) const { return t[i] != kEmpty ? 1u : 0u; }
+};
+
+// Gathers the occupied hash slots into dense keys re-encoded as (lo - base) << b | (hi - base).
+__global__ void k_hash_gather(const unsigned long long* __restrict__ table, long long cap,
+                              const unsigned* __restrict__ pos, const int* range, int b,
+                              uint64_t* __restrict__ keys) {
+  const int base = range[0];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cap;
+       i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long k = table[i];
+    if (k == kEmpty) continue;
+    const int lo = (int)((uint32_t)(k >> 32) ^ 0x80000000u);
+    const int hi = (int)((uint32_t)k ^ 0x80000000u);
+    const uint32_t dlo = (uint32_t)lo - (uint32_t)base, dhi = (uint32_t)hi - (uint32_t)base;
+    keys[pos[i]] = ((uint64_t)dlo << b) | (uint64_t)dhi;
+  }
+}
+
+__global__ void k_pairs_decode(const uint64_t* __restrict__ keys, long long m, const int* range,
+                               int b, int* __restrict__ out) {
+  const int base = range[0];
+  const uint64_t lowmask = (b >= 64) ? ~0ull : ((1ull << b) - 1ull);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (long long)gridDim.x * blockDim.x) {
+    const uint64_t k = keys[i];
+    out[2 * i] = (int)((uint32_t)(k >> b) + (uint32_t)base);
+    out[2 * i + 1] = (int)((uint32_t)(k & lowmask) + (uint32_t)base);
+  }
+}
+
+// ---- 7. pores (pore_extraction.hpp:107-127) -----------------------------------------------------
+// The SDF^2-weighted centroid with every float operation rounded exactly as the reference's
+// sequence: w = max(v,0)^2; sw += w; p* += d* w in dz->dy->dx order; f = p/sw if sw > 1e-6.
+__device__ __forceinline__ pnm_pore make_pore(const float* __restrict__ sdf, Dims d, int ix,
+                                              int iy, int iz, float ox, float oy, float oz,
+                                              float sx, float sy, float sz, float radius) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  float sw = 0.0f, px = 0.0f, py = 0.0f, pz = 0.0f;
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const long long u = ((long long)wrap1(iz + dz, nz) * ny + wrap1(iy + dy, ny)) * nx +
+                            wrap1(ix + dx, nx);
+        const float v = __ldg(&sdf[u]);
+        float w = v > 0.0f ? v : 0.0f;
+        w = __fmul_rn(w, w);
+        sw = __fadd_rn(sw, w);
+        px = __fadd_rn(px, __fmul_rn((float)dx, w));
+        py = __fadd_rn(py, __fmul_rn((float)dy, w));
+        pz = __fadd_rn(pz, __fmul_rn((float)dz, w));
+      }
+  float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+  if (sw > 1e-6f) {
+    fx = __fdiv_rn(px, sw);
+    fy = __fdiv_rn(py, sw);
+    fz = __fdiv_rn(pz, sw);
+  }
+  pnm_pore p;
+  p.x = __fadd_rn(ox, __fmul_rn(__fadd_rn((float)ix, fx), sx));
+  p.y = __fadd_rn(oy, __fmul_rn(__fadd_rn((float)iy, fy), sy));
+  p.z = __fadd_rn(oz, __fmul_rn(__fadd_rn((float)iz, fz), sz));
+  p.radius = radius;
+  return p;
+}
+
+// One thread per bitmap word: set bits are peaks in voxel order; pore r = prefix rank.
+__global__ void k_pores_emit(const float* __restrict__ sdf, Dims d, const uint32_t* __restrict__ bits,
+                             const unsigned* __restrict__ pref, long long words, float ox, float oy,
+                             float oz, float sx, float sy, float sz, pnm_pore* __restrict__ out,
+                             long long cap) {
+  const int nx = d.nx, ny = d.ny;
+  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < words;
+       w += (long long)gridDim.x * blockDim.x) {
+    uint32_t b = bits[w];
+    unsigned r = pref[w];
+    while (b) {
+      const int j = __ffs(b) - 1;
+      b &= b - 1;
+      if ((long long)r < cap) {
+        const long long v = w * 32 + j;
+        const int ix = (int)(v % nx), iy = (int)((v / nx) % ny), iz = (int)(v / ((long long)nx * ny));
+        out[r] = make_pore(sdf, d, ix, iy, iz, ox, oy, oz, sx, sy, sz, __ldg(&sdf[v]));
+      }
+      ++r;
+    }
+  }
+}
+
+// =================================================================================================
+// host stages
+// =================================================================================================
+namespace {
+inline unsigned grid_for(long long work, int threads, int sm_count, int per_sm = 8) {
+  long long b = (work + threads - 1) / threads;
+  const long long cap = (long long)sm_count * per_sm;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+inline dim3 tile_grid(Dims d) {
+  return dim3((unsigned)((d.nx + TX - 1) / TX), (unsigned)((d.ny + TY - 1) / TY),
+              (unsigned)((d.nz + TZ - 1) / TZ));
+}
+inline float marker_threshold(const float spacing[3]) {
+  const float min_sp = std::min(spacing[0], std::min(spacing[1], spacing[2]));
+  return -1.5f * min_sp;  // pore_extraction.hpp:163-164
+}
+}  // namespace
+
+Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st) {
+  const long long n = d.n();
+  const long long words = (n + 31) / 32;
+  st->d = d;
+  st->sdf = d_sdf;
+  PNM_TRY(c.buf(S_CODE, n, &st->code));
+  int* L = nullptr;
+  PNM_TRY(c.buf(S_L, n, &L));
+  PNM_TRY(c.buf(S_PEAKBITS, words, &st->peakbits));
+  PNM_CUDA(cudaMemsetAsync(st->peakbits, 0, words * sizeof(uint32_t), c.stream));
+  k_sdf_pass<<<tile_grid(d), TX * TY, 0, c.stream>>>(d_sdf, d, marker_threshold(spacing),
+                                                     st->code, L, st->peakbits);
+  PNM_CUDA(cudaGetLastError());
+  st->idtab = L;
+  return Status::ok();
+}
+
+Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st) {
+  const long long n = d.n();
+  const long long words = (n + 31) / 32;
+  cudaStream_t s = c.stream;
+  PNM_CUDA(cudaMemsetAsync(c.d_cnt, 0, CNT_COUNT * sizeof(unsigned), s));
+  PNM_TRY(run_sdf_pass(c, d_sdf, d, spacing, st));
+  int* L = st->idtab;
+  int *key, *keylist, *f0, *f1, *tmp;
+  PNM_TRY(c.buf(S_KEY, n, &key));
+  PNM_TRY(c.buf(S_KEYLIST, n, &keylist));
+  PNM_TRY(c.buf(S_FRONT0, n, &f0));
+  PNM_TRY(c.buf(S_FRONT1, n, &f1));
+  PNM_TRY(c.buf(S_TMP, n, &tmp));
+  st->key = key;
+
+  k_ccl_boundary<<<tile_grid(d), TX * TY, 0, s>>>(d, L, &c.d_cnt[CNT_ERR]);
+  PNM_CUDA(cudaGetLastError());
+  k_resolve<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, st->code, L, key, keylist, f0,
+                                                          c.d_cnt);
+  PNM_CUDA(cudaGetLastError());
+
+  // BFS-layer flood, in batches of sweeps between host checks (empty sweeps are no-ops)
+  const unsigned fgrid = grid_for(n, 256, c.sm_count, 4);
+  int* fin = f0;
+  int* fout = f1;
+  int cin = CNT_FRONT0, cout = CNT_FRONT1;
+  bool publish = false;
+  const int kBatch = 4, kMaxSweeps = 1 << 20;
+  int sweeps = 0;
+  while (true) {
+    for (int b = 0; b < kBatch; ++b) {
+      PNM_CUDA(cudaMemsetAsync(&c.d_cnt[cout], 0, sizeof(unsigned), s));
+      k_flood_discover<<<fgrid, 256, 0, s>>>(d, st->code, key, L, fin, &c.d_cnt[cin], tmp,
+                                             publish ? 1 : 0, fout, &c.d_cnt[cout], c.d_cnt);
+      k_flood_assign<<<fgrid, 256, 0, s>>>(d, key, fout, &c.d_cnt[cout], tmp);
+      std::swap(fin, fout);
+      std::swap(cin, cout);
+      publish = true;
+      ++sweeps;
+    }
+    PNM_CUDA(cudaGetLastError());
+    PNM_TRY(c.read_counters());
+    if (c.h_cnt[cin] == 0) break;
+    if (sweeps > kMaxSweeps) return Status{PNM_ERR_NOT_CONVERGED, "flood did not converge"};
+  }
+  st->flood_sweeps = sweeps;
+
+  // renumbering
+  uint32_t *firstP, *firstS;
+  unsigned *prefP, *prefS, *scan0;
+  PNM_TRY(c.buf(S_FIRSTP, words, &firstP));
+  PNM_TRY(c.buf(S_FIRSTS, words, &firstS));
+  PNM_TRY(c.buf(S_PREFP, words + 1, &prefP));
+  PNM_TRY(c.buf(S_PREFS, words + 1, &prefS));
+  PNM_TRY(c.buf(S_SCAN0, words / SCAN_TILE + 2, &scan0));
+  PNM_CUDA(cudaMemsetAsync(firstP, 0, words * 4, s));
+  PNM_CUDA(cudaMemsetAsync(firstS, 0, words * 4, s));
+  const unsigned nkeys = c.h_cnt[CNT_KEYS];
+  const unsigned kgrid = grid_for(nkeys, 256, c.sm_count);
+  k_key_first<<<kgrid, 256, 0, s>>>(keylist, &c.d_cnt[CNT_KEYS], L, st->code, firstP, firstS);
+  exclusive_scan(PopcountOf{firstP}, words, prefP, scan0, s);
+  exclusive_scan(PopcountOf{firstS}, words, prefS, scan0, s);
+  k_key_id<<<kgrid, 256, 0, s>>>(keylist, &c.d_cnt[CNT_KEYS], L, st->code, firstP, prefP, firstS,
+                                 prefS);
+  PNM_CUDA(cudaGetLastError());
+  unsigned tot[2];
+  PNM_CUDA(cudaMemcpyAsync(&tot[0], prefP + words, 4, cudaMemcpyDeviceToHost, s));
+  PNM_CUDA(cudaMemcpyAsync(&tot[1], prefS + words, 4, cudaMemcpyDeviceToHost, s));
+  PNM_CUDA(cudaStreamSynchronize(s));
+  st->n_pore_labels = (int)tot[0];
+  st->n_solid_labels = (int)tot[1];
+  if (c.h_cnt[CNT_ERR] & ERRF_UF_LIMIT)
+    return Status{PNM_ERR_NOT_CONVERGED, "union-find exceeded its iteration limit"};
+  return Status::ok();
+}
+
+namespace {
+Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int32_t* d_seg_in,
+                  int32_t* d_seg_out, bool want_pairs, long long cap_hint, int32_t** d_pairs_out,
+                  int64_t* n_pairs) {
+  cudaStream_t s = c.stream;
+  const long long n = d.n();
+  long long cap = 4096;
+  while (cap < cap_hint) cap <<= 1;
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    unsigned long long* table = nullptr;
+    int* range = nullptr;
+    PNM_TRY(c.buf(S_HASH, want_pairs ? cap : 1, &table));
+    PNM_TRY(c.buf(S_MAXBITS, 2, &range));
+    if (want_pairs) PNM_CUDA(cudaMemsetAsync(table, 0xff, cap * sizeof(unsigned long long), s));
+    const int init[2] = {INT_MAX, INT_MIN};
+    PNM_CUDA(cudaMemcpyAsync(range, init, sizeof(init), cudaMemcpyHostToDevice, s));
+    PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_ERR], 0, sizeof(unsigned), s));
+    PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_FLOW_SPARE1], 0, sizeof(unsigned), s));
+    const unsigned g = grid_for(n, 256, c.sm_count, 8);
+    if (from_keys)
+      k_seg_topo<<<g, 256, 0, s>>>(d, KeyLabels{st->key, st->idtab}, d_seg_out, want_pairs ? 1 : 0,
+                                   table, (uint64_t)(cap - 1), c.d_cnt, range);
+    else
+      k_seg_topo<<<g, 256, 0, s>>>(d, SegLabels{d_seg_in}, d_seg_out, want_pairs ? 1 : 0, table,
+                                   (uint64_t)(cap - 1), c.d_cnt, range);
+    PNM_CUDA(cudaGetLastError());
+    if (!want_pairs) return Status::ok();
+    PNM_TRY(c.read_counters());
+    if (c.h_cnt[CNT_ERR] & ERRF_HASH_FULL) {
+      cap <<= 2;
+      continue;
+    }
+    const long long m = c.h_cnt[CNT_FLOW_SPARE1];
+    *n_pairs = m;
+    int32_t* out = nullptr;
+    PNM_TRY(c.buf(S_PAIRS, 2 * m + 2, &out));
+    *d_pairs_out = out;
+    if (m == 0) return Status::ok();
+    int hr[2];
+    PNM_CUDA(cudaMemcpyAsync(hr, range, sizeof(hr), cudaMemcpyDeviceToHost, s));
+    PNM_CUDA(cudaStreamSynchronize(s));
+    const unsigned long long span = (unsigned long long)((long long)hr[1] - (long long)hr[0]);
+    int b = 1;
+    while (b < 32 && (1ull << b) <= span) ++b;
+    unsigned *pos, *scan0, *hist;
+    uint64_t *ka, *kb;
+    PNM_TRY(c.buf(S_SCAN1, cap + 1, &pos));
+    PNM_TRY(c.buf(S_SCAN0, cap / SCAN_TILE + 2 + (256 * (m / RS_TILE + 1)) / SCAN_TILE + 2, &scan0));
+    PNM_TRY(c.buf(S_KEYS_A, m, &ka));
+    PNM_TRY(c.buf(S_KEYS_B, m, &kb));
+    PNM_TRY(c.buf(S_RSHIST, 256 * (m / RS_TILE + 1) + 1, &hist));
+    exclusive_scan(Occupied{table}, cap, pos, scan0, s);
+    k_hash_gather<<<grid_for(cap, 256, c.sm_count), 256, 0, s>>>(table, cap, pos, range, b, ka);
+    const bool in_b = radix_sort(ka, nullptr, kb, nullptr, m, 0, 2 * b, hist, scan0, s);
+    k_pairs_decode<<<grid_for(m, 256, c.sm_count), 256, 0, s>>>(in_b ? kb : ka, m, range, b, out);
+    PNM_CUDA(cudaGetLastError());
+    return Status::ok();
+  }
+  return Status{PNM_ERR_INTERNAL, "pair hash set kept overflowing"};
+}
+}  // namespace
+
+Status run_seg_and_topology(Ctx& c, const SegState& st, int32_t* d_seg, bool want_pairs,
+                            int32_t** d_pairs_out, int64_t* n_pairs) {
+  const long long labels = (long long)st.n_pore_labels + st.n_solid_labels + 2;
+  const long long hint = std::min<long long>(std::max<long long>(64 * labels, 4096), 3 * st.d.n() + 64);
+  return emit_pairs(c, st.d, true, &st, nullptr, d_seg, want_pairs, hint, d_pairs_out, n_pairs);
+}
+
+Status run_topology_of_seg(Ctx& c, const int32_t* d_seg, Dims d, int32_t** d_pairs_out,
+                           int64_t* n_pairs) {
+  const long long hint = std::min<long long>(std::max<long long>(d.n() / 8, 4096), 3 * d.n() + 64);
+  return emit_pairs(c, d, false, nullptr, d_seg, nullptr, true, hint, d_pairs_out, n_pairs);
+}
+
+Status run_pores(Ctx& c, const SegState& st, const float origin[3], const float spacing[3],
+                 pnm_pore* d_out, int64_t cap, int64_t* n_pores) {
+  cudaStream_t s = c.stream;
+  const long long words = (st.d.n() + 31) / 32;
+  unsigned *pref, *scan0;
+  PNM_TRY(c.buf(S_PEAKPREF, words + 1, &pref));
+  PNM_TRY(c.buf(S_SCAN1, words / SCAN_TILE + 2, &scan0));
+  exclusive_scan(PopcountOf{st.peakbits}, words, pref, scan0, s);
+  k_pores_emit<<<grid_for(words, 256, c.sm_count), 256, 0, s>>>(
+      st.sdf, st.d, st.peakbits, pref, words, origin[0], origin[1], origin[2], spacing[0],
+      spacing[1], spacing[2], d_out, cap);
+  PNM_CUDA(cudaGetLastError());
+  unsigned tot = 0;
+  PNM_CUDA(cudaMemcpyAsync(&tot, pref + words, 4, cudaMemcpyDeviceToHost, s));
+  PNM_CUDA(cudaStreamSynchronize(s));
+  *n_pores = tot;
+  return Status::ok();
+}
+
+}  // namespace pnm

@@ -1,0 +1,90 @@
+"""Seeded parity cases shared by the oracle tests (CPU) and the GPU parity tests.
+
+Each case is (name, sdf (Nz,Ny,Nx) float32, origin_zyx, spacing_zyx). They cover the edge cases
+the reference's semantics hinge on: periodic wrap aliasing on dims 1-3, plateaus and ties broken
+by the wrapped index, sdf == 0 debris, NaN / inf values, all-pore / all-solid volumes, gradient
+walks longer than the 512-step cap, and flood wavefronts many layers deep.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from peclet_pnm_gb300 import synthetic as syn
+
+UNIT = ([0.0, 0.0, 0.0], [1.0, 1.0, 1.0])
+
+
+def _tent(n):
+    x = np.arange(n, dtype=np.float32)
+    return (np.float32(1.0) + np.minimum(x, np.float32(n) - x)).astype(np.float32)
+
+
+def edge_cases():
+    rng = np.random.default_rng(11)
+    out = []
+    for shp in [(1, 1, 1), (1, 1, 2), (2, 2, 2), (1, 3, 5), (3, 1, 4), (2, 5, 3), (4, 4, 1),
+                (3, 3, 3), (1, 7, 9), (5, 2, 6)]:
+        a = rng.normal(0.0, 2.0, size=shp).astype(np.float32)
+        out.append((f"tiny_{'x'.join(map(str, shp))}", a, *UNIT))
+    # plateaus: integer-valued SDF, ties everywhere
+    pk = syn.packing((24, 20, 28), 0.45, mean_r=5.0, seed=21)
+    out.append(("plateau_floor", np.floor(pk).astype(np.float32), *UNIT))
+    out.append(("plateau_round_half", (np.round(pk * 2) / 2).astype(np.float32), *UNIT))
+    # constant volumes
+    out.append(("all_pore_const", np.ones((6, 5, 7), np.float32), *UNIT))
+    out.append(("all_marker_const", np.full((5, 6, 4), -5.0, np.float32), *UNIT))
+    out.append(("all_flood_const", np.full((4, 5, 6), -0.5, np.float32), *UNIT))
+    out.append(("all_zero", np.zeros((5, 4, 6), np.float32), *UNIT))
+    # sdf == 0 band: debris
+    z = pk.copy()
+    z[np.abs(z) < 0.8] = 0.0
+    out.append(("zero_band", z.astype(np.float32), *UNIT))
+    # NaN / inf sprinkled
+    q = syn.packing((16, 18, 20), 0.4, mean_r=4.0, seed=22).astype(np.float32)
+    idx = rng.choice(q.size, size=40, replace=False)
+    q.reshape(-1)[idx[:15]] = np.nan
+    q.reshape(-1)[idx[15:28]] = np.inf
+    q.reshape(-1)[idx[28:]] = -np.inf
+    out.append(("nan_inf", q, *UNIT))
+    # gradient walks longer than 512 steps (a 1-D tent: the ascent from x=1 needs ~600 moves)
+    out.append(("walk_cap_line", _tent(1200).reshape(1, 1, 1200), *UNIT))
+    out.append(("walk_cap_plateau", np.ones((1, 1, 700), np.float32), *UNIT))
+    out.append(("walk_cap_2d", np.tile(_tent(1100), (2, 1)).reshape(1, 2, 1100), *UNIT))
+    # deep flood: a floodable serpentine sheet fed by one marker blob (many BFS layers)
+    s = np.full((6, 40, 40), 2.0, np.float32)
+    s[2:4, :, :] = -0.5
+    s[2:4, ::4, 5:] = 2.0
+    s[2:4, 2::4, :35] = 2.0
+    s[1:5, 0:3, 0:3] = -4.0
+    out.append(("deep_flood_serpentine", s, *UNIT))
+    # random noise (many tiny components) with anisotropic spacing and an origin
+    out.append(("noise_16_aniso", rng.normal(0.0, 1.5, size=(16, 17, 18)).astype(np.float32),
+                [0.25, -3.0, 7.5], [0.7, 1.3, 2.1]))
+    # thin spacing: marker threshold scales with min spacing
+    out.append(("packing_fine_spacing", pk.astype(np.float32) * 0.1, [0.0, 0.0, 0.0],
+                [0.1, 0.1, 0.25]))
+    return out
+
+
+def standard_cases():
+    return [
+        ("ci_lattice", syn.ci_lattice(), *UNIT),
+        ("sphere_lattice_36x30x24", syn.sphere_lattice(36, 30, 24), *UNIT),
+        ("trig_32_aniso", syn.trig_field(32, 32, 32), [0.5, 2.0, -1.0], [2.0, 1.0, 0.5]),
+        ("random_spheres_64", syn.random_spheres().astype(np.float32), *UNIT),
+        ("chamber_tube", syn.chamber_tube(), *UNIT),
+        ("capsules", syn.capsules(), *UNIT),
+        ("packing_40x48x56", syn.packing((40, 48, 56), 0.4, seed=7), *UNIT),
+    ]
+
+
+def flow_fields(sdf, seed=5):
+    """Random-normal MAC fields (u, v, w, p) and openness in [0, 1] with exact zeros."""
+    rng = np.random.default_rng(seed)
+    sh = sdf.shape
+    f = [np.ascontiguousarray(rng.normal(0.0, 1e-3, size=sh)) for _ in range(4)]
+    o = []
+    for _ in range(3):
+        x = rng.uniform(-0.3, 1.0, size=sh)
+        o.append(np.ascontiguousarray(np.clip(x, 0.0, 1.0)))
+    return f + o
