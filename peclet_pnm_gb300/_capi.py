@@ -24,7 +24,7 @@ PNM_ERR_NO_DEVICE = 6
 PNM_ERR_INTERNAL = 7
 
 if not os.path.exists(LIB_PATH):
-    raise ImportError(f"{LIB_PATH} is not built; run `python -m peclet_pnm_gb300.build` "
+    raise ImportError(f"{LIB_PATH} is not built; run `python peclet_pnm_gb300/build.py` "
                       "(no CPU fallback exists)")
 
 lib = ctypes.CDLL(LIB_PATH)

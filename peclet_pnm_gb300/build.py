@@ -1,7 +1,9 @@
 """Builds libpnm_gb300.so in-tree: nvcc for sm_103a, one object per translation unit, compiled
 in parallel, then linked. No CPU fallback is built.
 
-    python -m peclet_pnm_gb300.build          # or peclet_pnm_gb300.build.build()
+    python peclet_pnm_gb300/build.py [--force] [-v]
+
+Run it by path (or load it with importlib): importing the package requires the library.
 """
 from __future__ import annotations
 

@@ -20,7 +20,8 @@ def pytest_configure(config):
     if not os.path.exists(os.path.join(ROOT, "oracle", "libpnm_oracle.so")):
         subprocess.run(["bash", os.path.join(ROOT, "oracle", "build.sh")], check=True)
     if not os.path.exists(os.path.join(ROOT, "peclet_pnm_gb300", "libpnm_gb300.so")):
-        subprocess.run([sys.executable, "-m", "peclet_pnm_gb300.build"], cwd=ROOT, check=True)
+        subprocess.run([sys.executable, os.path.join(ROOT, "peclet_pnm_gb300", "build.py")],
+                       cwd=ROOT, check=True)
 
 
 @pytest.fixture(scope="session")
