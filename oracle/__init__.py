@@ -234,9 +234,14 @@ def reference_available() -> bool:
 
 
 def sorted_pores(p: np.ndarray) -> np.ndarray:
-    """Pores as a set: rows sorted lexicographically by (x, y, z, radius) bit patterns."""
-    p = np.asarray(p, np.float32).reshape(-1, 4)
+    """Pores as a set: rows sorted lexicographically by (x, y, z, radius). NaNs are replaced by
+    one canonical quiet NaN (the payload and sign of a NaN differ between x86, Arm and the GPU and
+    carry no meaning), so bitwise comparison of the result treats NaN as equal to NaN."""
+    p = np.array(p, np.float32).reshape(-1, 4)
     if len(p) == 0:
         return p
+    p[np.isnan(p)] = np.float32(np.nan)
+    bits = p.view(np.int32)
+    bits[np.isnan(p)] = 0x7FC00000
     order = np.lexsort((p[:, 3], p[:, 2], p[:, 1], p[:, 0]))
     return p[order]
