@@ -47,8 +47,8 @@ enum Counter : int {
   CNT_KEYS,          // distinct basin / solid keys seen (keylist length)
   CNT_FRONT0,        // flood frontier length, ping
   CNT_FRONT1,        // flood frontier length, pong
-  CNT_FRONT_SPARE,
-  CNT_FACE_REC,      // network flow: emitted flux records
+  CNT_FRONT_SPARE,   // flood voxels without a marker neighbour (list U)
+  CNT_EDGES,         // marker-CCL edges emitted by the SDF pass
   CNT_FLOW_SPARE0,
   CNT_FLOW_SPARE1,
   CNT_COUNT = 32
@@ -62,7 +62,7 @@ enum Slot : int {
   // network flow
   S_U, S_V, S_W, S_P, S_OX, S_OY, S_OZ, S_FLOWLAB, S_FBITS, S_FCORE, S_FPREF, S_FID, S_FPAIR,
   S_FPAR, S_FFILM, S_FMINCORE, S_FLABEL, S_ROOTFLAG, S_SLOTOF, S_PEAK, S_NPORES_OUT,
-  S_PPRES, S_REC, S_ACC, S_TDP, S_THROATS, S_MAXBITS, S_FLOWOUT,
+  S_PPRES, S_REC, S_ACC, S_TDP, S_THROATS, S_MAXBITS, S_FLOWOUT, S_ULIST, S_EDGES,
   S_COUNT
 };
 
@@ -121,6 +121,9 @@ struct SegState {
   int32_t* key = nullptr;       // per voxel: basin root (>=0), ~solid label (<0), INT_MIN none
   int32_t* idtab = nullptr;     // per key voxel: final signed label id
   uint32_t* peakbits = nullptr; // bitmap of extract_pores peaks
+  int2* edges = nullptr;        // marker-CCL edges (run head, neighbouring run representative)
+  unsigned edge_cap = 0;
+  unsigned n_edges = 0;
   int n_pore_labels = 0;        // np
   int n_solid_labels = 0;
   int flood_sweeps = 0;

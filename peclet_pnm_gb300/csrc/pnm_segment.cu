@@ -22,23 +22,36 @@ constexpr int TX = 32, TY = 8, TZ = 8;  // SDF-pass tile: 2048 voxels, 256 threa
 constexpr int kBig = INT_MAX;           // unset min-index / non-marker parent
 
 // ---- 1. SDF pass ---------------------------------------------------------------------------
-// Per voxel, from a shared-memory tile with a one-voxel periodic halo:
+// One warp = one 32-voxel x-row chunk of a 32x8x8 tile held in shared memory with a one-voxel
+// periodic halo. Per voxel:
 //  * ascent direction = lexicographic max of (sdf, wrapped index) over the voxel and its 26
 //    neighbours, scanned dz->dy->dx with the reference's comparisons (pore_extraction.hpp:284-304,
-//    :632-644); equal to "strict local max" when it points at the voxel itself (:93-104);
-//  * class (marker :177, flood :245-248, pore :276), flood seed (a marker neighbour);
-//  * peak bit for extract_pores (:89-106): !(sdf <= 0) and the voxel is its own ascent target;
-//  * tile-local union-find of the markers over the 13 forward neighbours (:204-222), written to
-//    L as the global id of the tile-local root. Non-markers get L = kBig.
+//    :632-644); it points at the voxel itself exactly when the voxel is a strict local max
+//    (:93-104);
+//  * class (marker :177, flood :245-248, pore :276) and flood seed (has a marker neighbour);
+//  * peak bit for extract_pores (:89-106): !(sdf <= 0) and the voxel is its own ascent target.
+// Marker CCL (:181-230), first half: a marker's union-find parent is the first marker of its run
+// inside the chunk (from a ballot; runs are connected). Adjacency to the 13 forward neighbours
+// (:204-206) is emitted as edges (own run head, representative of the neighbouring run) for the
+// four forward rows and the chunk end, deduplicated across the warp; k_ccl_edges unites them.
+// Non-markers get L = kBig.
+struct EdgeBuf {
+  int2* e;
+  unsigned cap;
+};
+__device__ __forceinline__ void push_edge(const EdgeBuf& eb, unsigned* cnt, int a, int b) {
+  const unsigned pos = atomicAdd(&cnt[CNT_EDGES], 1u);
+  if (pos < eb.cap) eb.e[pos] = make_int2(a, b);
+}
+
 __global__ void __launch_bounds__(TX* TY)
     k_sdf_pass(const float* __restrict__ sdf, Dims d, float thr, uint8_t* __restrict__ code,
-               int* __restrict__ L, uint32_t* __restrict__ peakbits) {
+               int* __restrict__ L, uint32_t* __restrict__ peakbits, EdgeBuf eb, unsigned* cnt) {
   constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2, NT = TX * TY;
   __shared__ float s[HZ][HY][HX];
-  __shared__ int lab[TZ * TY * TX];
   __shared__ int wx[HX], wy[HY], wz[HZ];
   const int nx = d.nx, ny = d.ny, nz = d.nz;
-  const long long nxy = (long long)nx * ny;
+  const int nxy = nx * ny;
   const int X0 = blockIdx.x * TX, Y0 = blockIdx.y * TY, Z0 = blockIdx.z * TZ;
   const int t = threadIdx.x;
   if (t < HX) wx[t] = ((X0 - 1 + t) % nx + nx) % nx;
@@ -47,113 +60,127 @@ __global__ void __launch_bounds__(TX* TY)
   __syncthreads();
   for (int i = t; i < HX * HY * HZ; i += NT) {
     const int hx = i % HX, hy = (i / HX) % HY, hz = i / (HX * HY);
-    s[hz][hy][hx] = __ldg(&sdf[wz[hz] * nxy + (long long)wy[hy] * nx + wx[hx]]);
+    s[hz][hy][hx] = __ldg(&sdf[wz[hz] * nxy + wy[hy] * nx + wx[hx]]);
   }
   __syncthreads();
+  const int lane = t & 31;  // == tx (TX == 32)
   const int tx = t % TX, ty = t / TX;
   const int gx = X0 + tx, gy = Y0 + ty;
   const bool inxy = gx < nx && gy < ny;
   for (int tz = 0; tz < TZ; ++tz) {
     const int gz = Z0 + tz;
-    const int li = (tz * TY + ty) * TX + tx;
-    int lb = -1;
-    if (inxy && gz < nz) {
-      const long long ci = gz * nxy + (long long)gy * nx + gx;
+    const bool valid = inxy && gz < nz;
+    const int ci = gz * nxy + gy * nx + gx;
+    bool marker = false;
+    if (valid) {
       const float cv = s[tz + 1][ty + 1][tx + 1];
       float bv = cv;
-      long long best = ci;
-      int bdir = kSelf;
+      int bk = kSelf;
       bool mk_nb = false;
 #pragma unroll
-      for (int dz = -1; dz <= 1; ++dz)
-#pragma unroll
-        for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-          for (int dx = -1; dx <= 1; ++dx) {
-            const int k = (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1);
-            if (k == kSelf) continue;
-            const float nv = s[tz + 1 + dz][ty + 1 + dy][tx + 1 + dx];
-            const long long ni =
-                wz[tz + 1 + dz] * nxy + (long long)wy[ty + 1 + dy] * nx + wx[tx + 1 + dx];
-            if (nv > bv) {
-              bv = nv;
-              best = ni;
-              bdir = k;
-            } else if (nv == bv && ni > best) {
-              best = ni;
-              bdir = k;
-            }
-            mk_nb |= (nv < thr);
-          }
+      for (int k = 0; k < 27; ++k) {
+        if (k == kSelf) continue;
+        const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
+        const float nv = s[tz + 1 + dz][ty + 1 + dy][tx + 1 + dx];
+        if (nv > bv) {
+          bv = nv;
+          bk = k;
+        } else if (nv == bv) {  // tie: the larger wrapped index wins
+          const int ni = wz[tz + 1 + dz] * nxy + wy[ty + 1 + dy] * nx + wx[tx + 1 + dx];
+          const int bi = bk == kSelf ? ci
+                                     : wz[tz + 1 + bk / 9 - 1] * nxy +
+                                           wy[ty + 1 + (bk / 3) % 3 - 1] * nx +
+                                           wx[tx + 1 + bk % 3 - 1];
+          if (ni > bi) bk = k;
+        }
+        mk_nb |= (nv < thr);
+      }
       const int cls = cv > 0.0f ? CLS_PORE
                                 : (cv < thr ? CLS_MARKER : (!(cv >= 0.0f) ? CLS_FLOOD : CLS_ZERO));
-      code[ci] = make_code(bdir, cls, cls == CLS_FLOOD && mk_nb);
-      if (!(cv <= 0.0f) && bdir == kSelf) atomicOr(&peakbits[ci >> 5], 1u << (ci & 31));
-      if (cls == CLS_MARKER) lb = li;
+      code[ci] = make_code(bk, cls, cls == CLS_FLOOD && mk_nb);
+      if (!(cv <= 0.0f) && bk == kSelf) atomicOr(&peakbits[ci >> 5], 1u << (ci & 31));
+      marker = cls == CLS_MARKER;
     }
-    lab[li] = lb;
-  }
-  __syncthreads();
-  // tile-local unions over the 13 forward neighbours that lie inside the tile and the volume
-  const int TXe = min(TX, nx - X0), TYe = min(TY, ny - Y0), TZe = min(TZ, nz - Z0);
-  for (int tz = 0; tz < TZ; ++tz) {
-    const int li = (tz * TY + ty) * TX + tx;
-    if (lab[li] == -1) continue;
+    // run heads inside the chunk
+    const unsigned mask = __ballot_sync(0xffffffffu, marker);
+    const unsigned starts = mask & ~(mask << 1);
+    const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+    const int head = marker ? gz * nxy + gy * nx + X0 + (31 - __clz(starts & upto)) : kBig;
+    if (valid) L[ci] = head;
+    // chunk end / volume end: the +x neighbour lies in another chunk (or wraps)
+    if (marker && (lane == 31 || gx + 1 == nx) && s[tz + 1][ty + 1][tx + 2] < thr)
+      push_edge(eb, cnt, head, gz * nxy + gy * nx + wx[tx + 2]);
+    // forward rows (dy,dz) = (1,0), (-1,1), (0,1), (1,1): runs of the 34-wide halo row window
 #pragma unroll
-    for (int k = 0; k < 13; ++k) {
-      const int dz = k < 9 ? 1 : 0;
-      const int dy = k < 9 ? (k / 3) - 1 : (k < 12 ? 1 : 0);
-      const int dx = k < 12 ? (k % 3) - 1 : 1;
-      const int lx = tx + dx, ly = ty + dy, lz = tz + dz;
-      if (lx < 0 || lx >= TXe || ly < 0 || ly >= TYe || lz >= TZe) continue;
-      const int lj = (lz * TY + ly) * TX + lx;
-      if (lab[lj] != -1) uf_unite_s(lab, li, lj);
+    for (int f = 0; f < 4; ++f) {
+      const int sy = ty + 1 + (f == 0 || f == 3 ? 1 : (f == 1 ? -1 : 0));
+      const int sz = tz + 1 + (f == 0 ? 0 : 1);
+      const unsigned lo = __ballot_sync(0xffffffffu, s[sz][sy][lane] < thr);
+      const unsigned hi = __ballot_sync(0xffffffffu, lane < 2 && s[sz][sy][32 + (lane & 1)] < thr);
+      const unsigned long long M = (unsigned long long)lo | ((unsigned long long)(hi & 3u) << 32);
+      const unsigned long long S = M & ~(M << 1);
+      int r0 = -1, r1 = -1;  // distinct window-run starts touching x-1..x+1
+      if (marker) {
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int hx = lane + 1 + dx;
+          if (!((M >> hx) & 1ull)) continue;
+          const int rs = 63 - __clzll((long long)(S & ((2ull << hx) - 1ull)));
+          if (rs != r0 && r0 >= 0 && rs != r1) r1 = rs;
+          if (r0 < 0) r0 = rs;
+        }
+      }
+      const int rowb = wz[sz] * nxy + wy[sy] * nx;
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int rs = j == 0 ? r0 : r1;
+        const unsigned long long pk =
+            rs >= 0 ? ((unsigned long long)(unsigned)head << 32) | (unsigned)(rowb + wx[rs]) : ~0ull;
+        const unsigned peers = __match_any_sync(0xffffffffu, pk);
+        if (pk != ~0ull && (__ffs(peers) - 1) == lane) push_edge(eb, cnt, head, rowb + wx[rs]);
+      }
     }
-  }
-  __syncthreads();
-  for (int tz = 0; tz < TZ; ++tz) {
-    const int gz = Z0 + tz;
-    if (!inxy || gz >= nz) continue;
-    const int li = (tz * TY + ty) * TX + tx;
-    const long long ci = gz * nxy + (long long)gy * nx + gx;
-    int out = kBig;
-    if (lab[li] != -1) {
-      const int r = uf_find_s(lab, li);
-      const int rx = r % TX, ry = (r / TX) % TY, rz = r / (TX * TY);
-      out = (int)((Z0 + rz) * nxy + (long long)(Y0 + ry) * nx + (X0 + rx));
-    }
-    L[ci] = out;
   }
 }
 
-// ---- 2. cross-tile CCL merge ------------------------------------------------------------------
-// Every marker voxel unites with those of its 13 forward periodic neighbours (the reference's
-// merge set, pore_extraction.hpp:204-206) that the tile-local pass did not see.
-__global__ void __launch_bounds__(TX* TY) k_ccl_boundary(Dims d, int* L, unsigned* err) {
+// ---- 2. marker CCL, second half ------------------------------------------------------------
+// Unites the emitted edges. The surviving root of a component is its minimum voxel id, the
+// reference's canonical label (pore_extraction.hpp:217-219).
+__global__ void __launch_bounds__(256) k_ccl_edges(const int2* __restrict__ e, const unsigned* n_p,
+                                                   unsigned cap, int* L, unsigned* err) {
+  const unsigned n = min(*n_p, cap);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int2 ab = e[i];
+    uf_unite(L, ab.x, ab.y, err);
+  }
+}
+
+// Fallback when the edge buffer overflowed (adversarial marker patterns): every marker unites
+// with its 13 forward periodic neighbours directly; lanes proposing the same (parent, parent)
+// link issue one union.
+__global__ void __launch_bounds__(256) k_ccl_all(Dims d, int* L, unsigned* err) {
+  const long long n = d.n();
   const int nx = d.nx, ny = d.ny, nz = d.nz;
-  const long long nxy = (long long)nx * ny;
-  const int X0 = blockIdx.x * TX, Y0 = blockIdx.y * TY, Z0 = blockIdx.z * TZ;
-  const int TXe = min(TX, nx - X0), TYe = min(TY, ny - Y0), TZe = min(TZ, nz - Z0);
-  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
-  if (tx >= TXe || ty >= TYe) return;
-  const bool edge_xy = tx == 0 || tx == TXe - 1 || ty == 0 || ty == TYe - 1;
-  const int gx = X0 + tx, gy = Y0 + ty;
-  for (int tz = 0; tz < TZe; ++tz) {
-    if (!edge_xy && tz != TZe - 1) continue;
-    const int gz = Z0 + tz;
-    const int ci = (int)(gz * nxy + (long long)gy * nx + gx);
-    if (L[ci] == kBig) continue;
-#pragma unroll
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
+       base += (long long)gridDim.x * blockDim.x) {
+    const long long vl = base + threadIdx.x;
+    const int v = (int)vl;
+    const int a = vl < n ? ld_relaxed(&L[v]) : kBig;
+    const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+#pragma unroll 1
     for (int k = 0; k < 13; ++k) {
       const int dz = k < 9 ? 1 : 0;
       const int dy = k < 9 ? (k / 3) - 1 : (k < 12 ? 1 : 0);
       const int dx = k < 12 ? (k % 3) - 1 : 1;
-      const int lx = tx + dx, ly = ty + dy, lz = tz + dz;
-      if (lx >= 0 && lx < TXe && ly >= 0 && ly < TYe && lz < TZe) continue;  // seen locally
-      const int ux = wrap1(gx + dx, nx), uy = wrap1(gy + dy, ny), uz = wrap1(gz + dz, nz);
-      const int u = (int)(uz * nxy + (long long)uy * nx + ux);
-      if (ld_relaxed(&L[u]) == kBig) continue;
-      uf_unite(L, ci, u, err);
+      unsigned long long pk = ~0ull;
+      int b = kBig;
+      if (a != kBig) {
+        b = ld_relaxed(&L[(wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx)]);
+        if (b != kBig && b != a) pk = ((unsigned long long)(unsigned)a << 32) | (unsigned)b;
+      }
+      const unsigned peers = __match_any_sync(0xffffffffu, pk);
+      if (pk != ~0ull && (__ffs(peers) - 1) == (int)lane_id()) uf_unite(L, a, b, err);
     }
   }
 }
@@ -176,50 +203,46 @@ __device__ __forceinline__ int chase_root(const uint8_t* __restrict__ code, int 
   return cur;
 }
 
-// For every voxel: marker -> key ~root(CCL) and the root joins the key list; pore -> key =
-// gradient root, atomicMin of the voxel id into L[root] (first-appearance index; pore voxels'
-// L started at kBig) and, on first touch, the root joins the key list; flood seed -> label =
-// min CCL root over its marker neighbours (the first Jacobi sweep, :250-258), queued as the
-// first BFS layer; everything else -> KEY_NONE.
+// For every voxel: marker -> key ~root(CCL), the root joins the key list; pore -> key = gradient
+// root, atomicMin of the voxel id into L[root] (its first-appearance index; pore voxels' L started
+// at kBig) and, on first touch, the root joins the key list; flood and zero voxels -> KEY_NONE
+// (flood labels follow in k_flood_seed). Lanes of a warp whose markers share a union-find parent
+// run one find for the group.
 __global__ void __launch_bounds__(256)
     k_resolve(Dims d, const uint8_t* __restrict__ code, int* L, int* __restrict__ key,
-              int* __restrict__ keylist, int* __restrict__ front, unsigned* cnt) {
+              int* __restrict__ keylist, unsigned* cnt) {
   const long long n = d.n();
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
   unsigned* err = &cnt[CNT_ERR];
   for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
        base += (long long)gridDim.x * blockDim.x) {
     const long long vl = base + threadIdx.x;
     const bool valid = vl < n;
     const int v = (int)vl;
-    int k = KEY_NONE, agg = -1;
-    bool new_key = false, seed = false;
+    int k = KEY_NONE, agg = -1, par = -1;
+    bool new_key = false;
     if (valid) {
       const uint8_t c = code[v];
       const int cls = code_cls(c);
       if (cls == CLS_MARKER) {
-        const int r = uf_find(L, v, err);
-        k = ~r;
-        new_key = (r == v);
+        par = ld_relaxed(&L[v]);
       } else if (cls == CLS_PORE) {
         const int r = chase_root(code, v, d);
         k = r;
         agg = r;
-      } else if (cls == CLS_FLOOD && code_seed(c)) {
-        const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
-        int best = INT_MAX;
-        for (int dz = -1; dz <= 1; ++dz)
-          for (int dy = -1; dy <= 1; ++dy)
-            for (int dx = -1; dx <= 1; ++dx) {
-              if (!dx && !dy && !dz) continue;
-              const int u = (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx);
-              if (code_cls(__ldg(&code[u])) == CLS_MARKER) best = min(best, uf_find(L, u, err));
-            }
-        k = ~best;
-        seed = true;
       }
-      key[v] = k;
     }
+    {  // one find per distinct parent in the warp
+      const unsigned peers = __match_any_sync(0xffffffffu, par);
+      const int leader = __ffs(peers) - 1;
+      int r = 0;
+      if (par >= 0 && (int)lane_id() == leader) r = uf_find(L, par, err);
+      r = __shfl_sync(0xffffffffu, r, leader);
+      if (par >= 0) {
+        k = ~r;
+        new_key = (r == v);
+      }
+    }
+    if (valid) key[v] = k;
     // warp-aggregated first-appearance minimum for pore basins: lanes hold consecutive voxel
     // ids, so the lowest lane of each same-root group carries the group minimum
     const unsigned peers = __match_any_sync(0xffffffffu, agg);
@@ -229,28 +252,100 @@ __global__ void __launch_bounds__(256)
     }
     const int kpos = warp_append(&cnt[CNT_KEYS], new_key);
     if (new_key) keylist[kpos] = (agg >= 0 ? agg : v);
-    const int fpos = warp_append(&cnt[CNT_FRONT0], seed);
-    if (seed) front[fpos] = v;
   }
 }
 
-// ---- 4. BFS-layer flood (the reference's Jacobi sweeps, pore_extraction.hpp:237-269) ------------
-// Layer t = unlabelled flood voxels adjacent to layer t-1; a layer-t voxel takes the smallest
-// label among its neighbours labelled in layers < t. Discovery marks layer t PENDING, assignment
-// computes labels into `tmp` (indexed like the frontier), and the next discovery publishes them,
-// so no voxel ever sees a same-layer label — exactly the double-buffered sweep.
+// ---- 4. flood of the shallow solid (the reference's Jacobi sweeps, pore_extraction.hpp:237-269) --
+// Sweep 1 labels every flood voxel next to a marker (a "seed") with the smallest neighbouring
+// marker label; sweep t labels the still-unlabelled flood voxels adjacent to sweep t-1's with the
+// smallest label among neighbours labelled before sweep t. Seeds are labelled from the markers'
+// final keys; the remaining flood voxels go to a list U, and deeper layers are discovered from U
+// (layer 2) and from each previous layer (t >= 3). Discovery marks a layer PENDING, assignment
+// computes its labels into `tmp`, and the next discovery publishes them, so no voxel ever sees a
+// same-sweep label — exactly the double-buffered Jacobi sweep.
+__global__ void __launch_bounds__(256)
+    k_flood_seed(Dims d, const uint8_t* __restrict__ code, int* key, int* L, int* __restrict__ ulist,
+                 unsigned* cnt) {
+  const long long n = d.n();
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
+       base += (long long)gridDim.x * blockDim.x) {
+    const long long vl = base + threadIdx.x;
+    const int v = (int)vl;
+    int lab = -1;
+    bool rest = false;
+    if (vl < n) {
+      const uint8_t c = code[v];
+      if (code_cls(c) == CLS_FLOOD) {
+        if (code_seed(c)) {
+          const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+          int bestk = INT_MIN;  // largest marker key == smallest label
+          for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy)
+              for (int dx = -1; dx <= 1; ++dx) {
+                if (!dx && !dy && !dz) continue;
+                const int u =
+                    (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx);
+                if (code_cls(__ldg(&code[u])) == CLS_MARKER) bestk = max(bestk, key[u]);
+              }
+          key[v] = bestk;
+          lab = ~bestk;
+        } else {
+          rest = true;
+        }
+      }
+    }
+    // first appearance of the solid label (label roots start at L[r] == r)
+    const unsigned peers = __match_any_sync(0xffffffffu, lab);
+    if (lab >= 0 && (__ffs(peers) - 1) == (int)lane_id()) atomicMin(&L[lab], v);
+    const int pos = warp_append(&cnt[CNT_FRONT_SPARE], rest);
+    if (rest) ulist[pos] = v;
+  }
+}
+
+// layer 2: listed flood voxels with a seed neighbour (they have no marker neighbour)
+__global__ void __launch_bounds__(256)
+    k_flood_layer2(Dims d, const uint8_t* __restrict__ code, int* key,
+                   const int* __restrict__ ulist, const unsigned* nu_p, int* __restrict__ fout,
+                   unsigned* nout_p) {
+  const unsigned nu = *nu_p;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nu;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int v = ulist[i];
+    const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+    bool hit = false;
+    for (int dz = -1; dz <= 1 && !hit; ++dz)
+      for (int dy = -1; dy <= 1 && !hit; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          if (!dx && !dy && !dz) continue;
+          const int u = (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx);
+          const uint8_t cu = __ldg(&code[u]);
+          if (code_cls(cu) == CLS_FLOOD && code_seed(cu)) {
+            hit = true;
+            break;
+          }
+        }
+    if (hit) {
+      key[v] = KEY_PENDING;
+      fout[atomicAdd(nout_p, 1u)] = v;
+    }
+  }
+}
+
+// publishes the labels of layer t (from tmp) and discovers layer t+1 among its neighbours
 __global__ void __launch_bounds__(256)
     k_flood_discover(Dims d, const uint8_t* __restrict__ code, int* key, int* L,
                      const int* __restrict__ fin, const unsigned* nin_p, const int* tmp,
-                     int publish, int* __restrict__ fout, unsigned* nout_p, unsigned* cnt) {
+                     int* __restrict__ fout, unsigned* nout_p) {
   const unsigned nin = *nin_p;
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nin;
        i += (long long)gridDim.x * blockDim.x) {
     const int v = fin[i];
-    const int lab = publish ? tmp[i] : ~key[v];
-    if (publish) key[v] = ~lab;
-    atomicMin(&L[lab], v);  // first appearance of the solid label (roots start at L[r] == r)
+    const int lab = tmp[i];
+    key[v] = ~lab;
+    atomicMin(&L[lab], v);
     const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
     for (int dz = -1; dz <= 1; ++dz)
       for (int dy = -1; dy <= 1; ++dy)
@@ -537,6 +632,7 @@ inline float marker_threshold(const float spacing[3]) {
 
 Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st) {
   const long long n = d.n();
+  PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_EDGES], 0, sizeof(unsigned), c.stream));
   const long long words = (n + 31) / 32;
   st->d = d;
   st->sdf = d_sdf;
@@ -545,8 +641,13 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
   PNM_TRY(c.buf(S_L, n, &L));
   PNM_TRY(c.buf(S_PEAKBITS, words, &st->peakbits));
   PNM_CUDA(cudaMemsetAsync(st->peakbits, 0, words * sizeof(uint32_t), c.stream));
+  EdgeBuf eb;
+  eb.cap = (unsigned)std::min<long long>(n / 4 + 4096, (long long)UINT_MAX - 1);
+  PNM_TRY(c.buf(S_EDGES, eb.cap, &eb.e));
+  st->edges = eb.e;
+  st->edge_cap = eb.cap;
   k_sdf_pass<<<tile_grid(d), TX * TY, 0, c.stream>>>(d_sdf, d, marker_threshold(spacing),
-                                                     st->code, L, st->peakbits);
+                                                     st->code, L, st->peakbits, eb, c.d_cnt);
   PNM_CUDA(cudaGetLastError());
   st->idtab = L;
   return Status::ok();
@@ -559,7 +660,8 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   PNM_CUDA(cudaMemsetAsync(c.d_cnt, 0, CNT_COUNT * sizeof(unsigned), s));
   PNM_TRY(run_sdf_pass(c, d_sdf, d, spacing, st));
   int* L = st->idtab;
-  int *key, *keylist, *f0, *f1, *tmp;
+  int *key, *keylist, *f0, *f1, *tmp, *ulist;
+  PNM_TRY(c.buf(S_ULIST, n, &ulist));
   PNM_TRY(c.buf(S_KEY, n, &key));
   PNM_TRY(c.buf(S_KEYLIST, n, &keylist));
   PNM_TRY(c.buf(S_FRONT0, n, &f0));
@@ -567,29 +669,39 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   PNM_TRY(c.buf(S_TMP, n, &tmp));
   st->key = key;
 
-  k_ccl_boundary<<<tile_grid(d), TX * TY, 0, s>>>(d, L, &c.d_cnt[CNT_ERR]);
+  k_ccl_edges<<<grid_for(n / 8 + 1, 256, c.sm_count), 256, 0, s>>>(
+      st->edges, &c.d_cnt[CNT_EDGES], st->edge_cap, L, &c.d_cnt[CNT_ERR]);
   PNM_CUDA(cudaGetLastError());
-  k_resolve<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, st->code, L, key, keylist, f0,
-                                                          c.d_cnt);
+  unsigned n_edges = 0;
+  PNM_CUDA(cudaMemcpyAsync(&n_edges, &c.d_cnt[CNT_EDGES], 4, cudaMemcpyDeviceToHost, s));
+  PNM_CUDA(cudaStreamSynchronize(s));
+  if (n_edges > st->edge_cap) {  // overflow: unite every forward adjacency directly
+    k_ccl_all<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, L, &c.d_cnt[CNT_ERR]);
+    PNM_CUDA(cudaGetLastError());
+  }
+  st->n_edges = n_edges;
+  k_resolve<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, st->code, L, key, keylist, c.d_cnt);
+  PNM_CUDA(cudaGetLastError());
+  k_flood_seed<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, st->code, key, L, ulist, c.d_cnt);
+  const unsigned fgrid = grid_for(n, 256, c.sm_count, 4);
+  k_flood_layer2<<<fgrid, 256, 0, s>>>(d, st->code, key, ulist, &c.d_cnt[CNT_FRONT_SPARE], f0,
+                                       &c.d_cnt[CNT_FRONT0]);
   PNM_CUDA(cudaGetLastError());
 
-  // BFS-layer flood, in batches of sweeps between host checks (empty sweeps are no-ops)
-  const unsigned fgrid = grid_for(n, 256, c.sm_count, 4);
+  // deeper layers, in batches of sweeps between host checks (empty sweeps are no-ops)
   int* fin = f0;
   int* fout = f1;
   int cin = CNT_FRONT0, cout = CNT_FRONT1;
-  bool publish = false;
   const int kBatch = 4, kMaxSweeps = 1 << 20;
-  int sweeps = 0;
+  int sweeps = 1;
   while (true) {
     for (int b = 0; b < kBatch; ++b) {
       PNM_CUDA(cudaMemsetAsync(&c.d_cnt[cout], 0, sizeof(unsigned), s));
-      k_flood_discover<<<fgrid, 256, 0, s>>>(d, st->code, key, L, fin, &c.d_cnt[cin], tmp,
-                                             publish ? 1 : 0, fout, &c.d_cnt[cout], c.d_cnt);
-      k_flood_assign<<<fgrid, 256, 0, s>>>(d, key, fout, &c.d_cnt[cout], tmp);
+      k_flood_assign<<<fgrid, 256, 0, s>>>(d, key, fin, &c.d_cnt[cin], tmp);
+      k_flood_discover<<<fgrid, 256, 0, s>>>(d, st->code, key, L, fin, &c.d_cnt[cin], tmp, fout,
+                                             &c.d_cnt[cout]);
       std::swap(fin, fout);
       std::swap(cin, cout);
-      publish = true;
       ++sweeps;
     }
     PNM_CUDA(cudaGetLastError());
