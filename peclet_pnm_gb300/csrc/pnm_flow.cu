@@ -412,10 +412,22 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-__global__ void k_face_flatten(long long M, int* par, unsigned* err) {
+// Roots of the face forest into a separate array: a read-only walk, so no store can overwrite a
+// flattened root with a stale ancestor (path-halving stores racing the final writes would).
+__global__ void k_face_flatten(long long M, const int* __restrict__ par, int* __restrict__ root,
+                               unsigned* err) {
   for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < M;
-       k += (long long)gridDim.x * blockDim.x)
-    par[k] = uf_find(par, (int)k, err);
+       k += (long long)gridDim.x * blockDim.x) {
+    int x = (int)k;
+    int it = 0;
+    for (; it < kUfLimit; ++it) {
+      const int p = par[x];
+      if (p == x) break;
+      x = p;
+    }
+    if (it == kUfLimit) atomicOr(err, ERRF_UF_LIMIT);
+    root[k] = x;
+  }
 }
 
 // Film attachment: a film component takes the smallest core-patch root adjacent to any of its
@@ -714,6 +726,8 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
   PNM_TRY(c.buf(S_FID, Mx, &fid));
   PNM_TRY(c.buf(S_FPAIR, Mx, &fpair));
   PNM_TRY(c.buf(S_FPAR, Mx, &par));
+  int* froot;
+  PNM_TRY(c.buf(S_FFILM, Mx, &froot));
   PNM_TRY(c.buf(S_FMINCORE, Mx, &minCore));
   PNM_TRY(c.buf(S_FLABEL, Mx, &label));
   PNM_TRY(c.buf(S_ROOTFLAG, Mx, &isroot));
@@ -728,7 +742,8 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
     k_face_compact<<<gridn(fwords, c.sm_count), 256, 0, s>>>(d, ifbits, ifpref, fwords, flowLab,
                                                              fid, fpair, par);
     k_face_unite<<<gridn(M, c.sm_count), 256, 0, s>>>(d, fx, fid, M, par, &c.d_cnt[CNT_ERR]);
-    k_face_flatten<<<gridn(M, c.sm_count), 256, 0, s>>>(M, par, &c.d_cnt[CNT_ERR]);
+    k_face_flatten<<<gridn(M, c.sm_count), 256, 0, s>>>(M, par, froot, &c.d_cnt[CNT_ERR]);
+    par = froot;  // every later reader wants the flattened roots
     k_fill_int<<<gridn(M, c.sm_count), 256, 0, s>>>(minCore, M, INT_MAX);
     k_film_attach<<<gridn(M, c.sm_count), 256, 0, s>>>(d, fx, fid, M, par, minCore);
     k_face_label<<<gridn(M, c.sm_count), 256, 0, s>>>(M, fx, fid, par, minCore, label, isroot);

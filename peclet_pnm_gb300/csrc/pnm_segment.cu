@@ -39,9 +39,22 @@ struct EdgeBuf {
   int2* e;
   unsigned cap;
 };
-__device__ __forceinline__ void push_edge(const EdgeBuf& eb, unsigned* cnt, int a, int b) {
-  const unsigned pos = atomicAdd(&cnt[CNT_EDGES], 1u);
-  if (pos < eb.cap) eb.e[pos] = make_int2(a, b);
+// Edges are staged in shared memory and reserved in the global buffer once per block (a single
+// global counter would serialise millions of same-address atomics); a full stage spills directly.
+constexpr int kEdgeStage = 2048;
+struct EdgeStage {
+  int2 e[kEdgeStage];
+  unsigned n;
+};
+__device__ __forceinline__ void push_edge(EdgeStage& st, const EdgeBuf& eb, unsigned* cnt, int a,
+                                          int b) {
+  const unsigned pos = atomicAdd(&st.n, 1u);
+  if (pos < (unsigned)kEdgeStage) {
+    st.e[pos] = make_int2(a, b);
+  } else {
+    const unsigned g = atomicAdd(&cnt[CNT_EDGES], 1u);
+    if (g < eb.cap) eb.e[g] = make_int2(a, b);
+  }
 }
 
 __global__ void __launch_bounds__(TX* TY)
@@ -50,10 +63,13 @@ __global__ void __launch_bounds__(TX* TY)
   constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2, NT = TX * TY;
   __shared__ float s[HZ][HY][HX];
   __shared__ int wx[HX], wy[HY], wz[HZ];
+  __shared__ EdgeStage stage;
+  __shared__ unsigned gbase;
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int nxy = nx * ny;
   const int X0 = blockIdx.x * TX, Y0 = blockIdx.y * TY, Z0 = blockIdx.z * TZ;
   const int t = threadIdx.x;
+  if (t == 0) stage.n = 0;
   if (t < HX) wx[t] = ((X0 - 1 + t) % nx + nx) % nx;
   if (t < HY) wy[t] = ((Y0 - 1 + t) % ny + ny) % ny;
   if (t < HZ) wz[t] = ((Z0 - 1 + t) % nz + nz) % nz;
@@ -109,7 +125,7 @@ __global__ void __launch_bounds__(TX* TY)
     if (valid) L[ci] = head;
     // chunk end / volume end: the +x neighbour lies in another chunk (or wraps)
     if (marker && (lane == 31 || gx + 1 == nx) && s[tz + 1][ty + 1][tx + 2] < thr)
-      push_edge(eb, cnt, head, gz * nxy + gy * nx + wx[tx + 2]);
+      push_edge(stage, eb, cnt, head, gz * nxy + gy * nx + wx[tx + 2]);
     // forward rows (dy,dz) = (1,0), (-1,1), (0,1), (1,1): runs of the 34-wide halo row window
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
@@ -137,10 +153,17 @@ __global__ void __launch_bounds__(TX* TY)
         const unsigned long long pk =
             rs >= 0 ? ((unsigned long long)(unsigned)head << 32) | (unsigned)(rowb + wx[rs]) : ~0ull;
         const unsigned peers = __match_any_sync(0xffffffffu, pk);
-        if (pk != ~0ull && (__ffs(peers) - 1) == lane) push_edge(eb, cnt, head, rowb + wx[rs]);
+        if (pk != ~0ull && (__ffs(peers) - 1) == lane)
+          push_edge(stage, eb, cnt, head, rowb + wx[rs]);
       }
     }
   }
+  __syncthreads();
+  const unsigned ns = min(stage.n, (unsigned)kEdgeStage);
+  if (t == 0) gbase = ns ? atomicAdd(&cnt[CNT_EDGES], ns) : 0u;
+  __syncthreads();
+  for (unsigned i = t; i < ns; i += NT)
+    if (gbase + i < eb.cap) eb.e[gbase + i] = stage.e[i];
 }
 
 // ---- 2. marker CCL, second half ------------------------------------------------------------
@@ -263,43 +286,66 @@ __global__ void __launch_bounds__(256)
 // (layer 2) and from each previous layer (t >= 3). Discovery marks a layer PENDING, assignment
 // computes its labels into `tmp`, and the next discovery publishes them, so no voxel ever sees a
 // same-sweep label — exactly the double-buffered Jacobi sweep.
-__global__ void __launch_bounds__(256)
-    k_flood_seed(Dims d, const uint8_t* __restrict__ code, int* key, int* L, int* __restrict__ ulist,
-                 unsigned* cnt) {
-  const long long n = d.n();
+__device__ __forceinline__ unsigned block_append(unsigned* cnt, bool take, unsigned* sh_base) {
+  // one global reservation per block: exclusive rank of `take` across the block
+  unsigned tot;
+  const unsigned r = block_exclusive_sum(take ? 1u : 0u, &tot);
+  if (threadIdx.x == 0) *sh_base = tot ? atomicAdd(cnt, tot) : 0u;
+  __syncthreads();
+  const unsigned b = *sh_base;
+  __syncthreads();
+  return b + r;
+}
+
+__global__ void __launch_bounds__(TX* TY)
+    k_flood_seed(Dims d, const uint8_t* __restrict__ code, int* __restrict__ key, int* L,
+                 int* __restrict__ ulist, unsigned* cnt) {
+  constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2, NT = TX * TY;
+  __shared__ int mk[HZ][HY][HX];  // marker neighbours' keys (~root), INT_MIN elsewhere
+  __shared__ int wx[HX], wy[HY], wz[HZ];
+  __shared__ unsigned sh_base;
   const int nx = d.nx, ny = d.ny, nz = d.nz;
-  for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
-       base += (long long)gridDim.x * blockDim.x) {
-    const long long vl = base + threadIdx.x;
-    const int v = (int)vl;
-    int lab = -1;
+  const int nxy = nx * ny;
+  const int X0 = blockIdx.x * TX, Y0 = blockIdx.y * TY, Z0 = blockIdx.z * TZ;
+  const int t = threadIdx.x;
+  if (t < HX) wx[t] = ((X0 - 1 + t) % nx + nx) % nx;
+  if (t < HY) wy[t] = ((Y0 - 1 + t) % ny + ny) % ny;
+  if (t < HZ) wz[t] = ((Z0 - 1 + t) % nz + nz) % nz;
+  __syncthreads();
+  for (int i = t; i < HX * HY * HZ; i += NT) {
+    const int hx = i % HX, hy = (i / HX) % HY, hz = i / (HX * HY);
+    const int g = wz[hz] * nxy + wy[hy] * nx + wx[hx];
+    (&mk[0][0][0])[i] = code_cls(__ldg(&code[g])) == CLS_MARKER ? __ldg(&key[g]) : INT_MIN;
+  }
+  __syncthreads();
+  const int tx = t % TX, ty = t / TX;
+  const int gx = X0 + tx, gy = Y0 + ty;
+  for (int tz = 0; tz < TZ; ++tz) {
+    const int gz = Z0 + tz;
+    const bool valid = gx < nx && gy < ny && gz < nz;
+    const int ci = gz * nxy + gy * nx + gx;
     bool rest = false;
-    if (vl < n) {
-      const uint8_t c = code[v];
+    if (valid) {
+      const uint8_t c = code[ci];
       if (code_cls(c) == CLS_FLOOD) {
         if (code_seed(c)) {
-          const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
           int bestk = INT_MIN;  // largest marker key == smallest label
-          for (int dz = -1; dz <= 1; ++dz)
-            for (int dy = -1; dy <= 1; ++dy)
-              for (int dx = -1; dx <= 1; ++dx) {
-                if (!dx && !dy && !dz) continue;
-                const int u =
-                    (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx);
-                if (code_cls(__ldg(&code[u])) == CLS_MARKER) bestk = max(bestk, key[u]);
-              }
-          key[v] = bestk;
-          lab = ~bestk;
+#pragma unroll
+          for (int k = 0; k < 27; ++k) {
+            if (k == kSelf) continue;
+            bestk = max(bestk, mk[tz + k / 9][ty + (k / 3) % 3][tx + k % 3]);
+          }
+          key[ci] = bestk;
+          const int lab = ~bestk;
+          // first appearance: the label's minimum starts at its root id L[lab] == lab
+          if (ci < lab) atomicMin(&L[lab], ci);
         } else {
           rest = true;
         }
       }
     }
-    // first appearance of the solid label (label roots start at L[r] == r)
-    const unsigned peers = __match_any_sync(0xffffffffu, lab);
-    if (lab >= 0 && (__ffs(peers) - 1) == (int)lane_id()) atomicMin(&L[lab], v);
-    const int pos = warp_append(&cnt[CNT_FRONT_SPARE], rest);
-    if (rest) ulist[pos] = v;
+    const unsigned pos = block_append(&cnt[CNT_FRONT_SPARE], rest, &sh_base);
+    if (rest) ulist[pos] = ci;
   }
 }
 
@@ -345,7 +391,7 @@ __global__ void __launch_bounds__(256)
     const int v = fin[i];
     const int lab = tmp[i];
     key[v] = ~lab;
-    atomicMin(&L[lab], v);
+    if (v < lab) atomicMin(&L[lab], v);  // a label's minimum starts at its root id
     const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
     for (int dz = -1; dz <= 1; ++dz)
       for (int dy = -1; dy <= 1; ++dy)
@@ -682,7 +728,7 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   st->n_edges = n_edges;
   k_resolve<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, st->code, L, key, keylist, c.d_cnt);
   PNM_CUDA(cudaGetLastError());
-  k_flood_seed<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, st->code, key, L, ulist, c.d_cnt);
+  k_flood_seed<<<tile_grid(d), TX * TY, 0, s>>>(d, st->code, key, L, ulist, c.d_cnt);
   const unsigned fgrid = grid_for(n, 256, c.sm_count, 4);
   k_flood_layer2<<<fgrid, 256, 0, s>>>(d, st->code, key, ulist, &c.d_cnt[CNT_FRONT_SPARE], f0,
                                        &c.d_cnt[CNT_FRONT0]);
