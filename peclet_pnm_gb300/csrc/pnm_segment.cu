@@ -146,16 +146,17 @@ __global__ void __launch_bounds__(TX* TY)
           if (r0 < 0) r0 = rs;
         }
       }
+      // lanes touching the same (own run, neighbouring run) pair are contiguous: emit only where
+      // the pair is new relative to the previous lane
       const int rowb = wz[sz] * nxy + wy[sy] * nx;
-#pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        const int rs = j == 0 ? r0 : r1;
-        const unsigned long long pk =
-            rs >= 0 ? ((unsigned long long)(unsigned)head << 32) | (unsigned)(rowb + wx[rs]) : ~0ull;
-        const unsigned peers = __match_any_sync(0xffffffffu, pk);
-        if (pk != ~0ull && (__ffs(peers) - 1) == lane)
-          push_edge(stage, eb, cnt, head, rowb + wx[rs]);
-      }
+      const int ph = __shfl_up_sync(0xffffffffu, head, 1);
+      const int p0 = __shfl_up_sync(0xffffffffu, r0, 1);
+      const int p1 = __shfl_up_sync(0xffffffffu, r1, 1);
+      const bool same_head = lane > 0 && ph == head;
+      if (r0 >= 0 && !(same_head && (r0 == p0 || r0 == p1)))
+        push_edge(stage, eb, cnt, head, rowb + wx[r0]);
+      if (r1 >= 0 && !(same_head && (r1 == p0 || r1 == p1)))
+        push_edge(stage, eb, cnt, head, rowb + wx[r1]);
     }
   }
   __syncthreads();
@@ -254,22 +255,25 @@ __global__ void __launch_bounds__(256)
         agg = r;
       }
     }
-    {  // one find per distinct parent in the warp
-      const unsigned peers = __match_any_sync(0xffffffffu, par);
-      const int leader = __ffs(peers) - 1;
+    const unsigned lane = lane_id();
+    {  // one find per run of lanes sharing a parent (lanes hold consecutive voxels)
+      const int pp = __shfl_up_sync(0xffffffffu, par, 1);
+      const bool lead = par >= 0 && (lane == 0 || pp != par);
+      const unsigned leaders = __ballot_sync(0xffffffffu, lead);
       int r = 0;
-      if (par >= 0 && (int)lane_id() == leader) r = uf_find(L, par, err);
-      r = __shfl_sync(0xffffffffu, r, leader);
+      if (lead) r = uf_find(L, par, err);
+      const int src = 31 - __clz(leaders & (lane == 31 ? 0xffffffffu : ((2u << lane) - 1u)));
+      r = __shfl_sync(0xffffffffu, r, src < 0 ? 0 : src);
       if (par >= 0) {
         k = ~r;
         new_key = (r == v);
       }
     }
     if (valid) key[v] = k;
-    // warp-aggregated first-appearance minimum for pore basins: lanes hold consecutive voxel
-    // ids, so the lowest lane of each same-root group carries the group minimum
-    const unsigned peers = __match_any_sync(0xffffffffu, agg);
-    if (agg >= 0 && (__ffs(peers) - 1) == (int)lane_id()) {
+    // first-appearance minimum for pore basins: the first lane of each run of lanes with the same
+    // root carries that run's minimum voxel id
+    const int pa = __shfl_up_sync(0xffffffffu, agg, 1);
+    if (agg >= 0 && (lane == 0 || pa != agg)) {
       const int old = atomicMin(&L[agg], v);
       if (old == kBig) new_key = true;
     }
@@ -546,8 +550,8 @@ __global__ void __launch_bounds__(256)
           lmax = max(lmax, max(s0, s1));
         }
       }
-      const unsigned peers = __match_any_sync(0xffffffffu, pk);
-      if (pk != kEmpty && (__ffs(peers) - 1) == (int)lane_id())
+      const uint64_t pp = __shfl_up_sync(0xffffffffu, pk, 1);
+      if (pk != kEmpty && (lane_id() == 0 || pp != pk))
         hash_insert(table, mask, pk, &cnt[CNT_ERR], &cnt[CNT_FLOW_SPARE1]);
     }
   }
