@@ -228,10 +228,10 @@ __global__ void k_centers_pressure(const float* __restrict__ sdf, Dims d, Geo g,
 // flow basins (:621-652): flowLab = seg at the <=512-step ascent root of EVERY cell. Pore voxels
 // already carry their root in key[]; other cells chase the ascent pointers.
 __global__ void __launch_bounds__(256)
-    k_flow_basins(Dims d, const uint8_t* __restrict__ code, const int* __restrict__ key,
-                  const int* __restrict__ seg, int* __restrict__ flowLab) {
+    k_flow_basins(Dims d, const uint8_t* __restrict__ code, const int* __restrict__ nxt,
+                  const int* __restrict__ key, const int* __restrict__ seg,
+                  int* __restrict__ flowLab) {
   const long long n = d.n();
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += (long long)gridDim.x * blockDim.x) {
     const uint8_t c0 = code[v];
@@ -239,15 +239,11 @@ __global__ void __launch_bounds__(256)
     if (code_cls(c0) == CLS_PORE) {
       root = key[v];
     } else {
-      int3 q = coords_of(v, nx, ny);
       int cur = (int)v;
       for (int s = 0; s < 512; ++s) {
-        const int dir = code_dir(__ldg(&code[cur]));
-        if (dir == kSelf) break;
-        q.x = wrap1(q.x + (dir % 3) - 1, nx);
-        q.y = wrap1(q.y + ((dir / 3) % 3) - 1, ny);
-        q.z = wrap1(q.z + (dir / 9) - 1, nz);
-        cur = (q.z * ny + q.y) * nx + q.x;
+        const int n2 = __ldg(&nxt[cur]);
+        if (n2 == cur) break;
+        cur = n2;
       }
       root = cur;
     }
@@ -686,7 +682,7 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
   }
   k_centers_pressure<<<gridn(np, c.sm_count), 256, 0, s>>>(st.sdf, d, geo, peak, np, in.p, pores,
                                                            ppres);
-  k_flow_basins<<<gridn(n, c.sm_count), 256, 0, s>>>(d, st.code, st.key, seg, flowLab);
+  k_flow_basins<<<gridn(n, c.sm_count), 256, 0, s>>>(d, st.code, st.nxt, st.key, seg, flowLab);
   PNM_CUDA(cudaGetLastError());
 
   // face classification + bounds

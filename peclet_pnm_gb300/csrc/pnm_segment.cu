@@ -59,7 +59,8 @@ __device__ __forceinline__ void push_edge(EdgeStage& st, const EdgeBuf& eb, unsi
 
 __global__ void __launch_bounds__(TX* TY)
     k_sdf_pass(const float* __restrict__ sdf, Dims d, float thr, uint8_t* __restrict__ code,
-               int* __restrict__ L, uint32_t* __restrict__ peakbits, EdgeBuf eb, unsigned* cnt) {
+               int* __restrict__ nxt, int* __restrict__ L, uint32_t* __restrict__ peakbits,
+               EdgeBuf eb, unsigned* cnt) {
   constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2, NT = TX * TY;
   __shared__ float s[HZ][HY][HX];
   __shared__ int wx[HX], wy[HY], wz[HZ];
@@ -89,31 +90,50 @@ __global__ void __launch_bounds__(TX* TY)
     const int ci = gz * nxy + gy * nx + gx;
     bool marker = false;
     if (valid) {
-      const float cv = s[tz + 1][ty + 1][tx + 1];
+      const float* c0 = &s[tz + 1][ty + 1][tx + 1];
+      const float cv = *c0;
       float bv = cv;
       int bk = kSelf;
-      bool mk_nb = false;
+      bool mk_nb = false, tie = false;
+      // fast scan with strict comparisons; any equality with the running maximum sends the voxel
+      // through the exact tie-aware scan below (identical result whenever no tie occurs)
 #pragma unroll
       for (int k = 0; k < 27; ++k) {
         if (k == kSelf) continue;
-        const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
-        const float nv = s[tz + 1 + dz][ty + 1 + dy][tx + 1 + dx];
+        const int off = (k / 9 - 1) * (HY * HX) + ((k / 3) % 3 - 1) * HX + (k % 3 - 1);
+        const float nv = c0[off];
+        tie |= (nv == bv);
         if (nv > bv) {
           bv = nv;
           bk = k;
-        } else if (nv == bv) {  // tie: the larger wrapped index wins
-          const int ni = wz[tz + 1 + dz] * nxy + wy[ty + 1 + dy] * nx + wx[tx + 1 + dx];
-          const int bi = bk == kSelf ? ci
-                                     : wz[tz + 1 + bk / 9 - 1] * nxy +
-                                           wy[ty + 1 + (bk / 3) % 3 - 1] * nx +
-                                           wx[tx + 1 + bk % 3 - 1];
-          if (ni > bi) bk = k;
         }
         mk_nb |= (nv < thr);
+      }
+      if (tie) {
+        bv = cv;
+        bk = kSelf;
+        int bi = ci;
+#pragma unroll 1
+        for (int k = 0; k < 27; ++k) {
+          if (k == kSelf) continue;
+          const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
+          const float nv = s[tz + 1 + dz][ty + 1 + dy][tx + 1 + dx];
+          const int ni = wz[tz + 1 + dz] * nxy + wy[ty + 1 + dy] * nx + wx[tx + 1 + dx];
+          if (nv > bv) {
+            bv = nv;
+            bk = k;
+            bi = ni;
+          } else if (nv == bv && ni > bi) {  // tie: the larger wrapped index wins
+            bk = k;
+            bi = ni;
+          }
+        }
       }
       const int cls = cv > 0.0f ? CLS_PORE
                                 : (cv < thr ? CLS_MARKER : (!(cv >= 0.0f) ? CLS_FLOOD : CLS_ZERO));
       code[ci] = make_code(bk, cls, cls == CLS_FLOOD && mk_nb);
+      nxt[ci] = bk == kSelf ? ci
+                            : wz[tz + bk / 9] * nxy + wy[ty + (bk / 3) % 3] * nx + wx[tx + bk % 3];
       if (!(cv <= 0.0f) && bk == kSelf) atomicOr(&peakbits[ci >> 5], 1u << (ci & 31));
       marker = cls == CLS_MARKER;
     }
@@ -126,6 +146,7 @@ __global__ void __launch_bounds__(TX* TY)
     // chunk end / volume end: the +x neighbour lies in another chunk (or wraps)
     if (marker && (lane == 31 || gx + 1 == nx) && s[tz + 1][ty + 1][tx + 2] < thr)
       push_edge(stage, eb, cnt, head, gz * nxy + gy * nx + wx[tx + 2]);
+    if (mask == 0) continue;  // warp-uniform: no marker in this row chunk
     // forward rows (dy,dz) = (1,0), (-1,1), (0,1), (1,1): runs of the 34-wide halo row window
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
@@ -212,17 +233,13 @@ __global__ void __launch_bounds__(256) k_ccl_all(Dims d, int* L, unsigned* err) 
 // ---- 3. resolve ----------------------------------------------------------------------------------
 // Gradient root of a voxel: follow the ascent pointers for at most 512 moves
 // (pore_extraction.hpp:277-309 and :626-648; MAX_STEPS = 512).
-__device__ __forceinline__ int chase_root(const uint8_t* __restrict__ code, int v, Dims d) {
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
-  int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+// (the ascent pointer of every voxel, as a voxel id, is nxt[]; a fixed point points at itself)
+__device__ __forceinline__ int chase_root(const int* __restrict__ nxt, int v) {
   int cur = v;
   for (int s = 0; s < 512; ++s) {
-    const int dir = code_dir(__ldg(&code[cur]));
-    if (dir == kSelf) break;
-    x = wrap1(x + (dir % 3) - 1, nx);
-    y = wrap1(y + ((dir / 3) % 3) - 1, ny);
-    z = wrap1(z + (dir / 9) - 1, nz);
-    cur = (z * ny + y) * nx + x;
+    const int n2 = __ldg(&nxt[cur]);
+    if (n2 == cur) break;
+    cur = n2;
   }
   return cur;
 }
@@ -233,8 +250,8 @@ __device__ __forceinline__ int chase_root(const uint8_t* __restrict__ code, int 
 // (flood labels follow in k_flood_seed). Lanes of a warp whose markers share a union-find parent
 // run one find for the group.
 __global__ void __launch_bounds__(256)
-    k_resolve(Dims d, const uint8_t* __restrict__ code, int* L, int* __restrict__ key,
-              int* __restrict__ keylist, unsigned* cnt) {
+    k_resolve(Dims d, const uint8_t* __restrict__ code, const int* __restrict__ nxt, int* L,
+              int* __restrict__ key, int* __restrict__ keylist, unsigned* cnt) {
   const long long n = d.n();
   unsigned* err = &cnt[CNT_ERR];
   for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
@@ -250,7 +267,7 @@ __global__ void __launch_bounds__(256)
       if (cls == CLS_MARKER) {
         par = ld_relaxed(&L[v]);
       } else if (cls == CLS_PORE) {
-        const int r = chase_root(code, v, d);
+        const int r = chase_root(nxt, v);
         k = r;
         agg = r;
       }
@@ -505,55 +522,62 @@ __device__ __forceinline__ void hash_insert(unsigned long long* table, uint64_t 
 struct KeyLabels {  // label of voxel v from key[] and the id table in L[]
   const int* key;
   const int* L;
-  __device__ int operator()(long long v) const { return label_of_key(L, __ldg(&key[v])); }
+  __device__ int operator()(int v) const { return label_of_key(L, __ldg(&key[v])); }
 };
 struct SegLabels {  // label of voxel v from a seg array
   const int* seg;
-  __device__ int operator()(long long v) const { return __ldg(&seg[v]); }
+  __device__ int operator()(int v) const { return __ldg(&seg[v]); }
 };
 
-// One pass: seg[v] (optional) and every differing (+x,+y,+z) periodic face pair into the hash set.
-// Identical pairs within a warp are merged before the global insert; lab_min/lab_max track the
-// label range for the sort.
+// One pass over 32 x 8 x 16 bricks (a warp owns a 32-voxel x-row and walks 16 z-planes): seg[v]
+// (optional) and every differing (+x,+y,+z) periodic face pair into the hash set. The +x label
+// comes from the neighbouring lane, the +z label is carried to the next plane. Lanes proposing
+// the pair of the previous lane skip their insert; lab_min/lab_max track the label range.
+constexpr int STX = 32, STY = 8, STZ = 16;
 template <class Lab>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(STX* STY)
     k_seg_topo(Dims d, Lab lab, int* __restrict__ seg, int want_pairs, unsigned long long* table,
                uint64_t mask, unsigned* cnt, int* range) {
-  const long long n = d.n();
   const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int lane = threadIdx.x & 31;
+  const int x = blockIdx.x * STX + lane;
+  const int y = blockIdx.y * STY + (threadIdx.x >> 5);
+  const int z0 = blockIdx.z * STZ, z1 = min(z0 + STZ, nz);
+  const bool in = x < nx && y < ny;
+  const int xp = x + 1 >= nx ? 0 : x + 1;
+  const int yp = y + 1 >= ny ? 0 : y + 1;
+  const int nxy = nx * ny;
   int lmin = INT_MAX, lmax = INT_MIN;
-  for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
-       base += (long long)gridDim.x * blockDim.x) {
-    const long long v = base + threadIdx.x;
-    const bool valid = v < n;
-    int s0 = 0;
-    int x = 0, y = 0, z = 0;
-    if (valid) {
-      s0 = lab(v);
-      if (seg) seg[v] = s0;
-      x = (int)(v % nx);
-      y = (int)((v / nx) % ny);
-      z = (int)(v / ((long long)nx * ny));
-    }
-    if (!want_pairs) continue;
+  int cur = in ? lab(z0 * nxy + y * nx + x) : 0;
+  for (int z = z0; z < z1; ++z) {
+    const int row = z * nxy + y * nx;
+    const int s0 = cur;
+    if (seg && in) seg[row + x] = s0;
+    const int zn = z + 1 >= nz ? 0 : z + 1;
+    int sz = 0;
+    if (in && (want_pairs || z + 1 < z1)) sz = lab(zn * nxy + y * nx + x);
+    if (want_pairs) {
+      int sx = __shfl_down_sync(0xffffffffu, s0, 1);
+      int sy = 0;
+      if (in) {
+        if (lane == 31 || x + 1 >= nx) sx = lab(row + xp);
+        sy = lab(z * nxy + yp * nx + x);
+      }
 #pragma unroll
-    for (int dd = 0; dd < 3; ++dd) {
-      uint64_t pk = kEmpty;
-      if (valid) {
-        const int ux = dd == 0 ? wrap1(x + 1, nx) : x;
-        const int uy = dd == 1 ? wrap1(y + 1, ny) : y;
-        const int uz = dd == 2 ? wrap1(z + 1, nz) : z;
-        const int s1 = lab(((long long)uz * ny + uy) * nx + ux);
-        if (s1 != s0) {
+      for (int dd = 0; dd < 3; ++dd) {
+        const int s1 = dd == 0 ? sx : (dd == 1 ? sy : sz);
+        uint64_t pk = kEmpty;
+        if (in && s1 != s0) {
           pk = pair_key(s0, s1);
           lmin = min(lmin, min(s0, s1));
           lmax = max(lmax, max(s0, s1));
         }
+        const uint64_t pp = __shfl_up_sync(0xffffffffu, pk, 1);
+        if (pk != kEmpty && (lane == 0 || pp != pk))
+          hash_insert(table, mask, pk, &cnt[CNT_ERR], &cnt[CNT_FLOW_SPARE1]);
       }
-      const uint64_t pp = __shfl_up_sync(0xffffffffu, pk, 1);
-      if (pk != kEmpty && (lane_id() == 0 || pp != pk))
-        hash_insert(table, mask, pk, &cnt[CNT_ERR], &cnt[CNT_FLOW_SPARE1]);
     }
+    cur = sz;
   }
   if (want_pairs) {
 #pragma unroll
@@ -561,7 +585,7 @@ __global__ void __launch_bounds__(256)
       lmin = min(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
       lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
     }
-    if (lane_id() == 0 && lmin <= lmax) {
+    if (lane == 0 && lmin <= lmax) {
       atomicMin(&range[0], lmin);
       atomicMax(&range[1], lmax);
     }
@@ -696,8 +720,10 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
   PNM_TRY(c.buf(S_EDGES, eb.cap, &eb.e));
   st->edges = eb.e;
   st->edge_cap = eb.cap;
+  PNM_TRY(c.buf(S_NXT, n, &st->nxt));
   k_sdf_pass<<<tile_grid(d), TX * TY, 0, c.stream>>>(d_sdf, d, marker_threshold(spacing),
-                                                     st->code, L, st->peakbits, eb, c.d_cnt);
+                                                     st->code, st->nxt, L, st->peakbits, eb,
+                                                     c.d_cnt);
   PNM_CUDA(cudaGetLastError());
   st->idtab = L;
   return Status::ok();
@@ -730,7 +756,8 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
     PNM_CUDA(cudaGetLastError());
   }
   st->n_edges = n_edges;
-  k_resolve<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, st->code, L, key, keylist, c.d_cnt);
+  k_resolve<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, st->code, st->nxt, L, key, keylist,
+                                                          c.d_cnt);
   PNM_CUDA(cudaGetLastError());
   k_flood_seed<<<tile_grid(d), TX * TY, 0, s>>>(d, st->code, key, L, ulist, c.d_cnt);
   const unsigned fgrid = grid_for(n, 256, c.sm_count, 4);
@@ -808,13 +835,15 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
     PNM_CUDA(cudaMemcpyAsync(range, init, sizeof(init), cudaMemcpyHostToDevice, s));
     PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_ERR], 0, sizeof(unsigned), s));
     PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_FLOW_SPARE1], 0, sizeof(unsigned), s));
-    const unsigned g = grid_for(n, 256, c.sm_count, 8);
+    const dim3 g((unsigned)((d.nx + STX - 1) / STX), (unsigned)((d.ny + STY - 1) / STY),
+                 (unsigned)((d.nz + STZ - 1) / STZ));
     if (from_keys)
-      k_seg_topo<<<g, 256, 0, s>>>(d, KeyLabels{st->key, st->idtab}, d_seg_out, want_pairs ? 1 : 0,
-                                   table, (uint64_t)(cap - 1), c.d_cnt, range);
+      k_seg_topo<<<g, STX * STY, 0, s>>>(d, KeyLabels{st->key, st->idtab}, d_seg_out,
+                                         want_pairs ? 1 : 0, table, (uint64_t)(cap - 1), c.d_cnt,
+                                         range);
     else
-      k_seg_topo<<<g, 256, 0, s>>>(d, SegLabels{d_seg_in}, d_seg_out, want_pairs ? 1 : 0, table,
-                                   (uint64_t)(cap - 1), c.d_cnt, range);
+      k_seg_topo<<<g, STX * STY, 0, s>>>(d, SegLabels{d_seg_in}, d_seg_out, want_pairs ? 1 : 0,
+                                         table, (uint64_t)(cap - 1), c.d_cnt, range);
     PNM_CUDA(cudaGetLastError());
     if (!want_pairs) return Status::ok();
     PNM_TRY(c.read_counters());
