@@ -1,0 +1,346 @@
+#!/usr/bin/env python
+"""Throughput of extract_pore_network on GB300 (Gvoxel/s), one JSON line on rank 0.
+
+Workload (one "step"): extract_pore_network on a 512^3 float32 SDF of polydisperse overlapping
+spheres (log-normal radii, mean 10 voxels, sigma 0.25, porosity 0.4, periodic min-image distance),
+seeded synthetic data generated on the device; outputs pores, int32 labels and connections.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value  : voxels / device time per step, SDF resident in HBM, results left on the device
+         (pnm_extract_pore_network_dev), timed with CUDA events on the library's stream.
+e2e    : the same metric through the host C ABI (pnm_extract_pore_network) from pinned host
+         memory: H2D of the SDF and D2H of labels, pores and pairs inside every timed step.
+roofline: the whole pipeline against the 64 B/voxel algorithmic model of the extraction path
+         (pores 4, markers+CCL 8, flood 12, gradient roots 8, renumbering 28, topology 4) and the
+         measured HBM copy bandwidth.
+N > 1  : independent replicas, one volume per rank (the path does not shard): scaling "weak".
+--impl reference: the reference's CPU implementation on this host's cores (the reference header
+         built against the Kokkos shim when present here, otherwise the project's CPU restatement),
+         each step a bounded sub-volume of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gvoxel/s extract_pore_network, batched vs plain on same GB300; p50/p99 latency"
+ALG_BYTES_PER_VOXEL = 64  # extract_pore_network algorithmic bytes per voxel
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=512, help="cube edge of the benchmark volume")
+    ap.add_argument("--cpu-sample", type=int, default=384,
+                    help="cube edge of the bounded CPU baseline sample")
+    ap.add_argument("--ref-sample", type=int, default=256,
+                    help="cube edge of one reference-arm step")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def measured_hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(p))["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per pipeline call from the committed ncu summary (profiles/), if present."""
+    p = os.path.join(ROOT, "profiles", "extract_pore_network_512_launches.txt")
+    try:
+        for line in open(p):
+            if line.startswith("dram_bytes_per_call:"):
+                return int(float(line.split(":")[1]))
+    except OSError:
+        pass
+    return None
+
+
+def workload_config(n_edge):
+    return {"workload": f"extract_pore_network {n_edge}^3 float32 polydisperse sphere packing",
+            "voxels": n_edge ** 3, "radius": "log-normal mean 10 voxels sigma 0.25",
+            "porosity": 0.4, "sdf": "periodic min-image, negative in solid", "seed": 2,
+            "l2": "SDF (4 B/voxel) and labels exceed the 129 MB L2 every step; no flush needed",
+            "parallelism": "replicas (one volume per GPU)"}
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[3:7]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def gen_volume(n_edge, seed, device):
+    from peclet_pnm_gb300 import synthetic as syn
+
+    return syn.packing((n_edge, n_edge, n_edge), 0.4, seed=seed, device=device)
+
+
+def cpu_sample_run(n_edge, threads, kind, sdf_np):
+    from oracle import Oracle
+
+    o = Oracle(kind, threads=threads, openmp_ref=True) if kind == "reference" else \
+        Oracle("port", threads=threads)
+    t = time.perf_counter()
+    o.extract_pore_network(sdf_np, [0.0] * 3, [1.0] * 3)
+    return time.perf_counter() - t
+
+
+def sample_volume(n_edge, seed):
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            return gen_volume(n_edge, seed, "cuda").cpu().numpy()
+    except Exception:
+        pass
+    return gen_volume(n_edge, seed, None)
+
+
+def reference_arm(args, rank):
+    if rank != 0:
+        return
+    from oracle import reference_available
+
+    kind = "reference" if reference_available() else "port"
+    threads = os.cpu_count() or 1
+    sdf = sample_volume(args.ref_sample, 2)
+    vox = sdf.size
+    for _ in range(args.warmup):
+        cpu_sample_run(args.ref_sample, threads, kind, sdf)
+    ts = [cpu_sample_run(args.ref_sample, threads, kind, sdf) for _ in range(args.steps)]
+    t = sum(ts) / len(ts)
+    value = vox / t / 1e9
+    sample = (f"{args.ref_sample}^3 sub-volume of the same packing generator per step "
+              f"({'reference header + Kokkos-compat OpenMP shim' if kind == 'reference' else 'C++ restatement of the reference algorithm, OpenMP'})")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gvoxel/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": workload_config(args.size),
+        "cpu_baseline": {"value": value, "unit": "Gvoxel/s", "cores": threads, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "Gvoxel/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}), flush=True)
+
+
+def ours(args, rank, world, local_rank):
+    import torch
+
+    import peclet_pnm_gb300 as pnm
+    from peclet_pnm_gb300 import _capi
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    n_edge = args.size
+    sdf = gen_volume(n_edge, 2 + rank, dev)
+    nvox = sdf.numel()
+    ctx = pnm.Context(local_rank)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    o = np.zeros(3, np.float32)
+    s = np.ones(3, np.float32)
+    pore_cap = 1_000_000
+    d_seg = torch.empty(nvox, dtype=torch.int32, device=dev)
+    d_pores = torch.empty((pore_cap, 4), dtype=torch.float32, device=dev)
+    npo, npa = _capi._i64(), _capi._i64()
+    pair_cap = 1 << 20
+    d_pairs = torch.empty((pair_cap, 2), dtype=torch.int32, device=dev)
+
+    def step():
+        rc = _capi.pnm_extract_pore_network_dev(
+            ctx.h, sdf.data_ptr(), n_edge, n_edge, n_edge, _capi.as_ptr(o), _capi.as_ptr(s),
+            d_pores.data_ptr(), pore_cap, ctypes.byref(npo), d_seg.data_ptr(),
+            d_pairs.data_ptr(), pair_cap, ctypes.byref(npa))
+        ctx.check(rc)
+
+    # size the pair buffer for this volume
+    rc = _capi.pnm_extract_pore_network_dev(
+        ctx.h, sdf.data_ptr(), n_edge, n_edge, n_edge, _capi.as_ptr(o), _capi.as_ptr(s),
+        d_pores.data_ptr(), pore_cap, ctypes.byref(npo), d_seg.data_ptr(), d_pairs.data_ptr(),
+        pair_cap, ctypes.byref(npa))
+    if rc == _capi.PNM_ERR_CAPACITY:
+        pair_cap = int(npa.value * 1.25) + 1024
+        d_pairs = torch.empty((pair_cap, 2), dtype=torch.int32, device=dev)
+    for _ in range(args.warmup):
+        step()
+    dist = world > 1
+    if dist:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(local_rank)
+    launches0 = ctx.stats()["launches"]
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    if dist:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    launches = ctx.stats()["launches"] - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    st = ctx.stats()
+    t = torch.tensor([ms], device=dev)
+    if dist:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = nvox * world / (ms_max * 1e-3) / 1e9
+
+    # e2e through the host C ABI from pinned memory
+    h_sdf = torch.empty(sdf.shape, dtype=torch.float32, pin_memory=True)
+    h_sdf.copy_(sdf.cpu())
+    h_seg = torch.empty(nvox, dtype=torch.int32, pin_memory=True)
+    pp = _capi._P(_capi.PnmPore)()
+    pr = _capi._P(ctypes.c_int32)()
+    npp, npr = _capi._i64(), _capi._i64()
+
+    def e2e_step():
+        ctx.check(_capi.pnm_extract_pore_network(
+            ctx.h, ctypes.c_void_p(h_sdf.data_ptr()), n_edge, n_edge, n_edge, _capi.as_ptr(o),
+            _capi.as_ptr(s), ctypes.byref(pp), ctypes.byref(npp),
+            ctypes.c_void_p(h_seg.data_ptr()), ctypes.byref(pr), ctypes.byref(npr)))
+        _capi.pnm_free(ctypes.cast(pp, ctypes.c_void_p))
+        _capi.pnm_free(ctypes.cast(pr, ctypes.c_void_p))
+
+    ctx.set_stream(None)
+    for _ in range(2):
+        e2e_step()
+    k_e2e = max(3, min(args.steps, 10))
+    if dist:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        e2e_step()
+    t_e2e = (time.perf_counter() - t0) / k_e2e
+    te = torch.tensor([t_e2e], device=dev)
+    if dist:
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = nvox * world / float(te.item()) / 1e9
+
+    peak, peak_src = measured_hbm_peak()
+    achieved = ALG_BYTES_PER_VOXEL * nvox / (ms * 1e-3) / 1e9
+    traffic = profile_traffic()
+    result = {
+        "metric": METRIC, "value": value, "unit": "Gvoxel/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": workload_config(n_edge),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "extract_pore_network device pipeline (all kernels of one call)",
+                     "model_bytes_per_voxel": ALG_BYTES_PER_VOXEL,
+                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"},
+        "e2e": {"value": e2e_value, "unit": "Gvoxel/s", "ms_per_step": t_e2e * 1e3,
+                "h2d_bytes_per_step": 4 * nvox,
+                "d2h_bytes_per_step": 4 * nvox + 16 * int(npp.value) + 8 * int(npr.value)},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "outputs": {"pores": int(st["n_pores"]), "pairs": int(st["n_pairs"]),
+                    "pore_labels": int(st["n_pore_labels"]),
+                    "solid_labels": int(st["n_solid_labels"]),
+                    "flood_sweeps": int(st["flood_sweeps"]), "ccl_edges": int(st["ccl_edges"])},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        samp = sdf.cpu().numpy()[:args.cpu_sample, :args.cpu_sample, :args.cpu_sample].copy()
+        t_cpu = cpu_sample_run(args.cpu_sample, threads, "port", samp)
+        result["cpu_baseline"] = {
+            "value": samp.size / t_cpu / 1e9, "unit": "Gvoxel/s", "cores": threads,
+            "kind": "port",
+            "sample": f"{args.cpu_sample}^3 corner of the benchmark volume, one "
+                      f"extract_pore_network ({t_cpu:.1f} s, C++ restatement with OpenMP)"}
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    ctx.close()
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        reference_arm(args, rank)
+        return
+    if world > 1:
+        import torch
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    try:
+        ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch
+
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -58,6 +58,22 @@ const char* pnm_execution_space(void);
 /* Frees buffers returned by the host entry points. */
 void pnm_free(void* p);
 
+/* Per-context statistics: cumulative counters and figures of the last call. */
+typedef struct {
+  int64_t launches;        /* CUDA kernels launched by this context since creation */
+  int64_t calls;           /* entry-point calls since creation */
+  int64_t voxels;          /* last call: nx*ny*nz */
+  int64_t ccl_edges;       /* last call: marker-CCL edges emitted by the SDF pass */
+  int32_t flood_sweeps;    /* last call: Jacobi flood sweeps run (incl. the empty final one) */
+  int32_t n_pore_labels;   /* last call: pore labels (np) */
+  int32_t n_solid_labels;  /* last call: solid labels */
+  int32_t reserved;
+  int64_t n_pores;         /* last call: extract_pores peaks */
+  int64_t n_pairs;         /* last call: unique connections */
+  int64_t workspace_bytes; /* device workspace currently held */
+} pnm_stats;
+int pnm_ctx_get_stats(const pnm_ctx* ctx, pnm_stats* out);
+
 /* ---- host-pointer entry points ------------------------------------------------------------ */
 
 /* extract_pores (pore_extraction.hpp:143 extract_pores_k; binding pnm_bindings.cpp:110-121).

@@ -47,6 +47,13 @@ class PnmFlowResult(ctypes.Structure):
                 ("throat_area", _P(ctypes.c_double)), ("throat_dp", _P(ctypes.c_double))]
 
 
+class PnmStats(ctypes.Structure):
+    _fields_ = [("launches", _i64), ("calls", _i64), ("voxels", _i64), ("ccl_edges", _i64),
+                ("flood_sweeps", _i32), ("n_pore_labels", _i32), ("n_solid_labels", _i32),
+                ("reserved", _i32), ("n_pores", _i64), ("n_pairs", _i64),
+                ("workspace_bytes", _i64)]
+
+
 def _sig(name, res, *args):
     f = getattr(lib, name)
     f.restype = res
@@ -60,6 +67,7 @@ pnm_last_error = _sig("pnm_last_error", ctypes.c_char_p, _vp)
 pnm_ctx_set_stream = _sig("pnm_ctx_set_stream", ctypes.c_int, _vp, _vp)
 pnm_ctx_trim = _sig("pnm_ctx_trim", ctypes.c_int, _vp)
 pnm_execution_space = _sig("pnm_execution_space", ctypes.c_char_p)
+pnm_ctx_get_stats = _sig("pnm_ctx_get_stats", ctypes.c_int, _vp, _P(PnmStats))
 pnm_free = _sig("pnm_free", None, _vp)
 pnm_extract_pores = _sig("pnm_extract_pores", ctypes.c_int, _vp, _vp, _i32, _i32, _i32, _vp, _vp,
                          _P(_P(PnmPore)), _P(_i64))
@@ -85,7 +93,7 @@ EXPORTED = ["pnm_ctx_create", "pnm_ctx_destroy", "pnm_last_error", "pnm_ctx_set_
             "pnm_ctx_trim", "pnm_execution_space", "pnm_free", "pnm_extract_pores",
             "pnm_segment_volume", "pnm_extract_topology", "pnm_extract_pore_network",
             "pnm_extract_network_flow", "pnm_flow_result_free", "pnm_extract_pore_network_dev",
-            "pnm_segment_volume_dev"]
+            "pnm_segment_volume_dev", "pnm_ctx_get_stats"]
 
 
 class PnmError(RuntimeError):
@@ -116,6 +124,11 @@ class Context:
 
     def trim(self):
         self.check(pnm_ctx_trim(self.h))
+
+    def stats(self) -> dict:
+        st = PnmStats()
+        self.check(pnm_ctx_get_stats(self.h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in PnmStats._fields_ if k != "reserved"}
 
     def close(self):
         if getattr(self, "h", None):

@@ -97,6 +97,7 @@ using pnm::Status;
 namespace {
 
 int finish(pnm_ctx* ctx, Status s) {
+  ++ctx->c.calls;
   if (!s.good()) ctx->c.last_error = s.msg;
   return s.code;
 }
@@ -131,13 +132,25 @@ Status do_pores(Ctx& c, const float* d_sdf, Dims d, const float* org, const floa
   return pnm::run_pores(c, st, org, spc, d_out, cap, n);
 }
 
+void record(Ctx& c, const pnm::SegState& st, int64_t n_pores, int64_t n_pairs) {
+  c.last.voxels = st.d.n();
+  c.last.ccl_edges = st.n_edges;
+  c.last.flood_sweeps = st.flood_sweeps;
+  c.last.n_pore_labels = st.n_pore_labels;
+  c.last.n_solid_labels = st.n_solid_labels;
+  c.last.n_pores = n_pores;
+  c.last.n_pairs = n_pairs;
+}
+
 Status do_network(Ctx& c, const float* d_sdf, Dims d, const float* org, const float* spc,
                   pnm_pore* d_pores, int64_t pore_cap, int64_t* n_pores, int32_t* d_seg,
                   bool want_pairs, int32_t** d_pairs, int64_t* n_pairs) {
   pnm::SegState st;
   PNM_TRY(pnm::run_segmentation(c, d_sdf, d, spc, &st));
   if (d_pores) PNM_TRY(pnm::run_pores(c, st, org, spc, d_pores, pore_cap, n_pores));
-  return pnm::run_seg_and_topology(c, st, d_seg, want_pairs, d_pairs, n_pairs);
+  PNM_TRY(pnm::run_seg_and_topology(c, st, d_seg, want_pairs, d_pairs, n_pairs));
+  record(c, st, d_pores ? *n_pores : 0, want_pairs ? *n_pairs : 0);
+  return Status::ok();
 }
 
 }  // namespace
@@ -192,6 +205,15 @@ void pnm_ctx_destroy(pnm_ctx* ctx) {
 }
 
 const char* pnm_last_error(const pnm_ctx* ctx) { return ctx ? ctx->c.last_error.c_str() : ""; }
+
+int pnm_ctx_get_stats(const pnm_ctx* ctx, pnm_stats* out) {
+  if (!ctx || !out) return PNM_ERR_ARG;
+  *out = ctx->c.last;
+  out->launches = ctx->c.launches;
+  out->calls = ctx->c.calls;
+  out->workspace_bytes = (int64_t)ctx->c.ws.total_bytes();
+  return PNM_OK;
+}
 
 int pnm_ctx_set_stream(pnm_ctx* ctx, void* stream) {
   if (!ctx) return PNM_ERR_ARG;
@@ -446,6 +468,7 @@ int pnm_extract_network_flow(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t
                        {grad_p_xyz[0], grad_p_xyz[1], grad_p_xyz[2]}};
     pnm::FlowOutputsHost o;
     PNM_TRY(pnm::run_network_flow(c, st, origin_xyz, spacing_xyz, in, &o));
+    record(c, st, 0, 0);
     auto* r = static_cast<pnm_flow_result*>(std::calloc(1, sizeof(pnm_flow_result)));
     if (!r) return Status{PNM_ERR_INTERNAL, "out of host memory"};
     r->n_pores = (int64_t)o.pores.size();

@@ -83,6 +83,9 @@ struct Ctx {
   unsigned* d_cnt = nullptr;  // CNT_COUNT device counters
   unsigned* h_cnt = nullptr;  // pinned host mirror
   int sm_count = 0;
+  long long launches = 0;   // kernels launched by this context (cumulative)
+  long long calls = 0;      // entry-point calls (cumulative)
+  pnm_stats last{};         // per-call statistics of the last call
   std::string last_error;
   Status fail(Status s) {
     last_error = s.msg;

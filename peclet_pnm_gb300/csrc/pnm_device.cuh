@@ -238,7 +238,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(F f, long long m, co
 
 // Exclusive scan: out[i] = sum_{j<i} f(j), out[m] = total. `tmp` needs ceil(m/TILE)+1 entries.
 template <class F>
-inline void exclusive_scan(F f, long long m, unsigned* out, unsigned* tmp, cudaStream_t s) {
+inline void exclusive_scan(F f, long long m, unsigned* out, unsigned* tmp, cudaStream_t s,
+                           long long* launches) {
   if (m <= 0) {
     cudaMemsetAsync(out, 0, sizeof(unsigned), s);
     return;
@@ -247,6 +248,7 @@ inline void exclusive_scan(F f, long long m, unsigned* out, unsigned* tmp, cudaS
   k_scan_reduce<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(f, m, tmp);
   k_scan_single<<<1, SCAN_THREADS, 0, s>>>(tmp, nb);
   k_scan_down<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(f, m, tmp, out);
+  *launches += 3;
 }
 
 struct PopcountOf {
@@ -327,7 +329,7 @@ static __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t
 // scan_tmp ceil(256*nb/SCAN_TILE)+1.
 inline bool radix_sort(uint64_t* ka, unsigned* va, uint64_t* kb, unsigned* vb, long long m,
                        int lo_bit, int hi_bit, unsigned* hist, unsigned* scan_tmp,
-                       cudaStream_t s) {
+                       cudaStream_t s, long long* launches) {
   if (m <= 1) return false;
   const long long nb = (m + RS_TILE - 1) / RS_TILE;
   bool in_b = false;
@@ -337,8 +339,9 @@ inline bool radix_sort(uint64_t* ka, unsigned* va, uint64_t* kb, unsigned* vb, l
     uint64_t* ko = in_b ? ka : kb;
     unsigned* vo = in_b ? va : vb;
     k_rs_hist<<<(unsigned)nb, RS_THREADS, 0, s>>>(ki, m, sh, hist);
-    exclusive_scan(ValueOf{hist}, 256 * nb, hist, scan_tmp, s);
+    exclusive_scan(ValueOf{hist}, 256 * nb, hist, scan_tmp, s, launches);
     k_rs_scatter<<<(unsigned)nb, RS_THREADS, 0, s>>>(ki, vi, ko, vo, m, sh, hist);
+    *launches += 2;
     in_b = !in_b;
   }
   return in_b;

@@ -674,15 +674,15 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
   PNM_TRY(c.buf(S_PPRES, np, &ppres));
   PNM_CUDA(cudaMemsetAsync(peak, 0, np * sizeof(int), s));
   const long long words = (n + 31) / 32;
-  k_peaks<<<gridn(words, c.sm_count), 256, 0, s>>>(st.peakbits, words, st.code, seg, peak);
+  k_peaks<<<gridn(words, c.sm_count), 256, 0, s>>>(st.peakbits, words, st.code, seg, peak); ++c.launches;
   Geo geo;
   for (int a = 0; a < 3; ++a) {
     geo.o[a] = origin[a];
     geo.s[a] = spacing[a];
   }
   k_centers_pressure<<<gridn(np, c.sm_count), 256, 0, s>>>(st.sdf, d, geo, peak, np, in.p, pores,
-                                                           ppres);
-  k_flow_basins<<<gridn(n, c.sm_count), 256, 0, s>>>(d, st.code, st.nxt, st.key, seg, flowLab);
+                                                           ppres); ++c.launches;
+  k_flow_basins<<<gridn(n, c.sm_count), 256, 0, s>>>(d, st.code, st.nxt, st.key, seg, flowLab); ++c.launches;
   PNM_CUDA(cudaGetLastError());
 
   // face classification + bounds
@@ -701,8 +701,8 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
                Az = (double)spacing[0] * spacing[1];  // :869-870
   const FieldPtrs fp{in.u, in.v, in.w, in.ox, in.oy, in.oz};
   k_face_class<<<gridn(n, c.sm_count), 256, 0, s>>>(d, st.code, flowLab, fp, Ax, Ay, Az, ifbits,
-                                                     corebits, bounds);
-  exclusive_scan(PopcountOf{ifbits}, fwords, ifpref, scan0, s);
+                                                     corebits, bounds); ++c.launches;
+  exclusive_scan(PopcountOf{ifbits}, fwords, ifpref, scan0, s, &c.launches);
   PNM_CUDA(cudaGetLastError());
   unsigned M32 = 0;
   unsigned long long hb[2];
@@ -736,14 +736,14 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
   while ((1ll << b) < (long long)np) ++b;  // pore labels 1..np -> (label-1) in b bits
   if (M > 0) {
     k_face_compact<<<gridn(fwords, c.sm_count), 256, 0, s>>>(d, ifbits, ifpref, fwords, flowLab,
-                                                             fid, fpair, par);
-    k_face_unite<<<gridn(M, c.sm_count), 256, 0, s>>>(d, fx, fid, M, par, &c.d_cnt[CNT_ERR]);
-    k_face_flatten<<<gridn(M, c.sm_count), 256, 0, s>>>(M, par, froot, &c.d_cnt[CNT_ERR]);
+                                                             fid, fpair, par); ++c.launches;
+    k_face_unite<<<gridn(M, c.sm_count), 256, 0, s>>>(d, fx, fid, M, par, &c.d_cnt[CNT_ERR]); ++c.launches;
+    k_face_flatten<<<gridn(M, c.sm_count), 256, 0, s>>>(M, par, froot, &c.d_cnt[CNT_ERR]); ++c.launches;
     par = froot;  // every later reader wants the flattened roots
-    k_fill_int<<<gridn(M, c.sm_count), 256, 0, s>>>(minCore, M, INT_MAX);
-    k_film_attach<<<gridn(M, c.sm_count), 256, 0, s>>>(d, fx, fid, M, par, minCore);
-    k_face_label<<<gridn(M, c.sm_count), 256, 0, s>>>(M, fx, fid, par, minCore, label, isroot);
-    exclusive_scan(IsRoot{isroot}, M, rpos, scan0, s);
+    k_fill_int<<<gridn(M, c.sm_count), 256, 0, s>>>(minCore, M, INT_MAX); ++c.launches;
+    k_film_attach<<<gridn(M, c.sm_count), 256, 0, s>>>(d, fx, fid, M, par, minCore); ++c.launches;
+    k_face_label<<<gridn(M, c.sm_count), 256, 0, s>>>(M, fx, fid, par, minCore, label, isroot); ++c.launches;
+    exclusive_scan(IsRoot{isroot}, M, rpos, scan0, s, &c.launches);
     PNM_CUDA(cudaGetLastError());
     unsigned nt32 = 0;
     PNM_CUDA(cudaMemcpyAsync(&nt32, rpos + M, 4, cudaMemcpyDeviceToHost, s));
@@ -764,10 +764,10 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
     PNM_TRY(c.buf(S_VALS_B, nt, &vb));
     PNM_TRY(c.buf(S_RSHIST, 256 * (nt / RS_TILE + 1) + 1, &hist));
     PNM_TRY(c.buf(S_SCAN1, (256 * (nt / RS_TILE + 1)) / SCAN_TILE + 2, &stmp));
-    k_root_keys<<<gridn(M, c.sm_count), 256, 0, s>>>(M, isroot, rpos, fpair, b, ka, va);
-    const bool in_b = radix_sort(ka, va, kb, vb, nt, 0, 2 * b, hist, stmp, s);
+    k_root_keys<<<gridn(M, c.sm_count), 256, 0, s>>>(M, isroot, rpos, fpair, b, ka, va); ++c.launches;
+    const bool in_b = radix_sort(ka, va, kb, vb, nt, 0, 2 * b, hist, stmp, s, &c.launches);
     k_slots<<<gridn(nt, c.sm_count), 256, 0, s>>>(nt, in_b ? kb : ka, in_b ? vb : va, b, slotOf,
-                                                  throats_d);
+                                                  throats_d); ++c.launches;
     PNM_CUDA(cudaGetLastError());
   }
 
@@ -799,7 +799,7 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
   unsigned long long* accCy = accCx + 2 * ntx;
   unsigned long long* accCz = accCy + 2 * ntx;
   k_flux<<<gridn(n, c.sm_count), 256, 0, s>>>(d, flowLab, fp, fx, label, slotOf, peak, P, accR,
-                                               accQ, accA, accCx, accCy, accCz);
+                                               accQ, accA, accCx, accCy, accCz); ++c.launches;
   double* dres;
   PNM_TRY(c.buf(S_FLOWOUT, nacc + ntx, &dres));
   double* resid = dres;
@@ -809,13 +809,13 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
   double* Cy = Cx + ntx;
   double* Cz = Cy + ntx;
   double* dp = Cz + ntx;
-  k_fixed_to_double<<<gridn(np, c.sm_count), 256, 0, s>>>(accR, np, P.sq, resid);
+  k_fixed_to_double<<<gridn(np, c.sm_count), 256, 0, s>>>(accR, np, P.sq, resid); ++c.launches;
   if (nt > 0) {
-    k_fixed_to_double<<<gridn(nt, c.sm_count), 256, 0, s>>>(accQ, nt, P.sq, Q);
-    k_fixed_to_double<<<gridn(nt, c.sm_count), 256, 0, s>>>(accA, nt, P.sa, A);
-    k_fixed_to_double<<<gridn(nt, c.sm_count), 256, 0, s>>>(accCx, nt, P.sc, Cx);
-    k_fixed_to_double<<<gridn(nt, c.sm_count), 256, 0, s>>>(accCy, nt, P.sc, Cy);
-    k_fixed_to_double<<<gridn(nt, c.sm_count), 256, 0, s>>>(accCz, nt, P.sc, Cz);
+    k_fixed_to_double<<<gridn(nt, c.sm_count), 256, 0, s>>>(accQ, nt, P.sq, Q); ++c.launches;
+    k_fixed_to_double<<<gridn(nt, c.sm_count), 256, 0, s>>>(accA, nt, P.sa, A); ++c.launches;
+    k_fixed_to_double<<<gridn(nt, c.sm_count), 256, 0, s>>>(accCx, nt, P.sc, Cx); ++c.launches;
+    k_fixed_to_double<<<gridn(nt, c.sm_count), 256, 0, s>>>(accCy, nt, P.sc, Cy); ++c.launches;
+    k_fixed_to_double<<<gridn(nt, c.sm_count), 256, 0, s>>>(accCz, nt, P.sc, Cz); ++c.launches;
     DpParams D;
     for (int a = 0; a < 3; ++a) {
       D.o[a] = origin[a];
@@ -825,7 +825,7 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
       D.g[a] = in.grad_p[a];
     }
     k_throat_dp<<<gridn(nt, c.sm_count), 256, 0, s>>>(nt, throats_d, pores, ppres, peak, A, Cx,
-                                                      Cy, Cz, D, dp);
+                                                      Cy, Cz, D, dp); ++c.launches;
   }
   PNM_CUDA(cudaGetLastError());
 

@@ -723,7 +723,7 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
   PNM_TRY(c.buf(S_NXT, n, &st->nxt));
   k_sdf_pass<<<tile_grid(d), TX * TY, 0, c.stream>>>(d_sdf, d, marker_threshold(spacing),
                                                      st->code, st->nxt, L, st->peakbits, eb,
-                                                     c.d_cnt);
+                                                     c.d_cnt); ++c.launches;
   PNM_CUDA(cudaGetLastError());
   st->idtab = L;
   return Status::ok();
@@ -746,23 +746,23 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   st->key = key;
 
   k_ccl_edges<<<grid_for(n / 8 + 1, 256, c.sm_count), 256, 0, s>>>(
-      st->edges, &c.d_cnt[CNT_EDGES], st->edge_cap, L, &c.d_cnt[CNT_ERR]);
+      st->edges, &c.d_cnt[CNT_EDGES], st->edge_cap, L, &c.d_cnt[CNT_ERR]); ++c.launches;
   PNM_CUDA(cudaGetLastError());
   unsigned n_edges = 0;
   PNM_CUDA(cudaMemcpyAsync(&n_edges, &c.d_cnt[CNT_EDGES], 4, cudaMemcpyDeviceToHost, s));
   PNM_CUDA(cudaStreamSynchronize(s));
   if (n_edges > st->edge_cap) {  // overflow: unite every forward adjacency directly
-    k_ccl_all<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, L, &c.d_cnt[CNT_ERR]);
+    k_ccl_all<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, L, &c.d_cnt[CNT_ERR]); ++c.launches;
     PNM_CUDA(cudaGetLastError());
   }
   st->n_edges = n_edges;
   k_resolve<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, st->code, st->nxt, L, key, keylist,
-                                                          c.d_cnt);
+                                                          c.d_cnt); ++c.launches;
   PNM_CUDA(cudaGetLastError());
-  k_flood_seed<<<tile_grid(d), TX * TY, 0, s>>>(d, st->code, key, L, ulist, c.d_cnt);
+  k_flood_seed<<<tile_grid(d), TX * TY, 0, s>>>(d, st->code, key, L, ulist, c.d_cnt); ++c.launches;
   const unsigned fgrid = grid_for(n, 256, c.sm_count, 4);
   k_flood_layer2<<<fgrid, 256, 0, s>>>(d, st->code, key, ulist, &c.d_cnt[CNT_FRONT_SPARE], f0,
-                                       &c.d_cnt[CNT_FRONT0]);
+                                       &c.d_cnt[CNT_FRONT0]); ++c.launches;
   PNM_CUDA(cudaGetLastError());
 
   // deeper layers, in batches of sweeps between host checks (empty sweeps are no-ops)
@@ -774,9 +774,9 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   while (true) {
     for (int b = 0; b < kBatch; ++b) {
       PNM_CUDA(cudaMemsetAsync(&c.d_cnt[cout], 0, sizeof(unsigned), s));
-      k_flood_assign<<<fgrid, 256, 0, s>>>(d, key, fin, &c.d_cnt[cin], tmp);
+      k_flood_assign<<<fgrid, 256, 0, s>>>(d, key, fin, &c.d_cnt[cin], tmp); ++c.launches;
       k_flood_discover<<<fgrid, 256, 0, s>>>(d, st->code, key, L, fin, &c.d_cnt[cin], tmp, fout,
-                                             &c.d_cnt[cout]);
+                                             &c.d_cnt[cout]); ++c.launches;
       std::swap(fin, fout);
       std::swap(cin, cout);
       ++sweeps;
@@ -800,11 +800,11 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   PNM_CUDA(cudaMemsetAsync(firstS, 0, words * 4, s));
   const unsigned nkeys = c.h_cnt[CNT_KEYS];
   const unsigned kgrid = grid_for(nkeys, 256, c.sm_count);
-  k_key_first<<<kgrid, 256, 0, s>>>(keylist, &c.d_cnt[CNT_KEYS], L, st->code, firstP, firstS);
-  exclusive_scan(PopcountOf{firstP}, words, prefP, scan0, s);
-  exclusive_scan(PopcountOf{firstS}, words, prefS, scan0, s);
+  k_key_first<<<kgrid, 256, 0, s>>>(keylist, &c.d_cnt[CNT_KEYS], L, st->code, firstP, firstS); ++c.launches;
+  exclusive_scan(PopcountOf{firstP}, words, prefP, scan0, s, &c.launches);
+  exclusive_scan(PopcountOf{firstS}, words, prefS, scan0, s, &c.launches);
   k_key_id<<<kgrid, 256, 0, s>>>(keylist, &c.d_cnt[CNT_KEYS], L, st->code, firstP, prefP, firstS,
-                                 prefS);
+                                 prefS); ++c.launches;
   PNM_CUDA(cudaGetLastError());
   unsigned tot[2];
   PNM_CUDA(cudaMemcpyAsync(&tot[0], prefP + words, 4, cudaMemcpyDeviceToHost, s));
@@ -844,6 +844,7 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
     else
       k_seg_topo<<<g, STX * STY, 0, s>>>(d, SegLabels{d_seg_in}, d_seg_out, want_pairs ? 1 : 0,
                                          table, (uint64_t)(cap - 1), c.d_cnt, range);
+    ++c.launches;
     PNM_CUDA(cudaGetLastError());
     if (!want_pairs) return Status::ok();
     PNM_TRY(c.read_counters());
@@ -870,10 +871,10 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
     PNM_TRY(c.buf(S_KEYS_A, m, &ka));
     PNM_TRY(c.buf(S_KEYS_B, m, &kb));
     PNM_TRY(c.buf(S_RSHIST, 256 * (m / RS_TILE + 1) + 1, &hist));
-    exclusive_scan(Occupied{table}, cap, pos, scan0, s);
-    k_hash_gather<<<grid_for(cap, 256, c.sm_count), 256, 0, s>>>(table, cap, pos, range, b, ka);
-    const bool in_b = radix_sort(ka, nullptr, kb, nullptr, m, 0, 2 * b, hist, scan0, s);
-    k_pairs_decode<<<grid_for(m, 256, c.sm_count), 256, 0, s>>>(in_b ? kb : ka, m, range, b, out);
+    exclusive_scan(Occupied{table}, cap, pos, scan0, s, &c.launches);
+    k_hash_gather<<<grid_for(cap, 256, c.sm_count), 256, 0, s>>>(table, cap, pos, range, b, ka); ++c.launches;
+    const bool in_b = radix_sort(ka, nullptr, kb, nullptr, m, 0, 2 * b, hist, scan0, s, &c.launches);
+    k_pairs_decode<<<grid_for(m, 256, c.sm_count), 256, 0, s>>>(in_b ? kb : ka, m, range, b, out); ++c.launches;
     PNM_CUDA(cudaGetLastError());
     return Status::ok();
   }
@@ -901,10 +902,10 @@ Status run_pores(Ctx& c, const SegState& st, const float origin[3], const float 
   unsigned *pref, *scan0;
   PNM_TRY(c.buf(S_PEAKPREF, words + 1, &pref));
   PNM_TRY(c.buf(S_SCAN1, words / SCAN_TILE + 2, &scan0));
-  exclusive_scan(PopcountOf{st.peakbits}, words, pref, scan0, s);
+  exclusive_scan(PopcountOf{st.peakbits}, words, pref, scan0, s, &c.launches);
   k_pores_emit<<<grid_for(words, 256, c.sm_count), 256, 0, s>>>(
       st.sdf, st.d, st.peakbits, pref, words, origin[0], origin[1], origin[2], spacing[0],
-      spacing[1], spacing[2], d_out, cap);
+      spacing[1], spacing[2], d_out, cap); ++c.launches;
   PNM_CUDA(cudaGetLastError());
   unsigned tot = 0;
   PNM_CUDA(cudaMemcpyAsync(&tot, pref + words, 4, cudaMemcpyDeviceToHost, s));
