@@ -145,6 +145,24 @@ int pnm_extract_pore_network_dev(pnm_ctx* ctx, const float* d_sdf, int32_t nx, i
 int pnm_segment_volume_dev(pnm_ctx* ctx, const float* d_sdf, int32_t nx, int32_t ny, int32_t nz,
                            const float spacing_xyz[3], int32_t* d_seg);
 
+/* ---- allocation-free entry point -------------------------------------------------------------
+ * No counterpart in the reference. extract_pores on a device SDF for callers that cannot let a
+ * library allocate device memory: frameworks that hand out every byte of device memory from
+ * their own pool under a fixed budget, and serving loops that must not enter the driver's
+ * allocator (cudaMalloc / cudaFree can synchronise the device) while other work is in flight.
+ * The caller passes the device SDF, a device output array of pore_cap pores and a stream
+ * (cudaStream_t as void*, NULL = default stream); results match pnm_extract_pores. The only
+ * scratch is a static device array of the library (about 16 MiB, held on every device that
+ * loads the library until the process exits), so volumes above 2^26 voxels (67,108,864, e.g.
+ * 406^3) are rejected with PNM_ERR_SHAPE. All calls on a device share that array: calls whose
+ * work overlaps on the GPU race and must be serialised. The first call on each device looks up
+ * the array's address; make it before any stream capture. Returns PNM_ERR_CAPACITY (with
+ * *n_pores = the count found) when pore_cap is too small. No context is used or needed. */
+int pnm_extract_pores_noalloc(const float* d_sdf, int32_t nx, int32_t ny, int32_t nz,
+                              const float origin_xyz[3], const float spacing_xyz[3],
+                              pnm_pore* d_pores, int64_t pore_cap, int64_t* n_pores,
+                              void* stream);
+
 #ifdef __cplusplus
 }
 #endif

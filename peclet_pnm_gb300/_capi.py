@@ -87,13 +87,15 @@ pnm_extract_network_flow = _sig("pnm_extract_network_flow", ctypes.c_int, _vp, _
                                 _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                 _P(_P(PnmFlowResult)))
 pnm_flow_result_free = _sig("pnm_flow_result_free", None, _P(PnmFlowResult))
+pnm_extract_pores_noalloc = _sig("pnm_extract_pores_noalloc", ctypes.c_int, _vp, _i32, _i32, _i32,
+                                 _vp, _vp, _vp, _i64, _P(_i64), _vp)
 
 #: every symbol include/pnm_gb300.h declares
 EXPORTED = ["pnm_ctx_create", "pnm_ctx_destroy", "pnm_last_error", "pnm_ctx_set_stream",
             "pnm_ctx_trim", "pnm_execution_space", "pnm_free", "pnm_extract_pores",
             "pnm_segment_volume", "pnm_extract_topology", "pnm_extract_pore_network",
             "pnm_extract_network_flow", "pnm_flow_result_free", "pnm_extract_pore_network_dev",
-            "pnm_segment_volume_dev", "pnm_ctx_get_stats"]
+            "pnm_segment_volume_dev", "pnm_ctx_get_stats", "pnm_extract_pores_noalloc"]
 
 
 class PnmError(RuntimeError):

@@ -144,6 +144,10 @@ Status run_topology_of_seg(Ctx& c, const int32_t* d_seg, Dims d, int32_t** d_pai
 // Compacts the peak bitmap into pores (voxel order, centroid-refined) in d_out (cap entries).
 Status run_pores(Ctx& c, const SegState& st, const float origin[3], const float spacing[3],
                  pnm_pore* d_out, int64_t cap, int64_t* n_pores);
+// Pore records from a peak bitmap and its exclusive word prefix counts (voxel order, <= cap).
+void launch_pores_emit(const float* sdf, Dims d, const uint32_t* bits, const unsigned* pref,
+                       long long words, const float origin[3], const float spacing[3],
+                       pnm_pore* out, long long cap, unsigned grid, cudaStream_t s);
 // SDF pass only (for extract_pores alone).
 Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st);
 

@@ -683,6 +683,13 @@ __global__ void k_pores_emit(const float* __restrict__ sdf, Dims d, const uint32
   }
 }
 
+void launch_pores_emit(const float* sdf, Dims d, const uint32_t* bits, const unsigned* pref,
+                       long long words, const float origin[3], const float spacing[3],
+                       pnm_pore* out, long long cap, unsigned grid, cudaStream_t s) {
+  k_pores_emit<<<grid, 256, 0, s>>>(sdf, d, bits, pref, words, origin[0], origin[1], origin[2],
+                                    spacing[0], spacing[1], spacing[2], out, cap);
+}
+
 // =================================================================================================
 // host stages
 // =================================================================================================
