@@ -463,7 +463,7 @@ int pnm_extract_network_flow(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t
       PNM_CUDA(cudaMemcpyAsync(df[i], hf[i], nb, cudaMemcpyHostToDevice, c.stream));
     }
     pnm::SegState st;
-    PNM_TRY(pnm::run_segmentation(c, d_sdf, d, spacing_xyz, &st));
+    PNM_TRY(pnm::run_segmentation(c, d_sdf, d, spacing_xyz, &st, /*all_ascent=*/true));
     pnm::FlowInputs in{df[0], df[1], df[2], df[3], df[4], df[5], df[6],
                        {grad_p_xyz[0], grad_p_xyz[1], grad_p_xyz[2]}};
     pnm::FlowOutputsHost o;

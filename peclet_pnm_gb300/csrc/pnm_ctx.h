@@ -133,8 +133,10 @@ struct SegState {
   int flood_sweeps = 0;
 };
 
-// Fused SDF pass + CCL + flood + gradient roots + first-appearance renumbering.
-Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st);
+// Fused SDF pass + CCL + flood + gradient roots + first-appearance renumbering. all_ascent:
+// also compute the ascent pointer of non-pore voxels (network flow's basins need every cell).
+Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st,
+                        bool all_ascent = false);
 // Writes seg (if d_seg != null) and the unique sorted label pairs (if want_pairs) from the state.
 Status run_seg_and_topology(Ctx& c, const SegState& st, int32_t* d_seg, bool want_pairs,
                             int32_t** d_pairs_out, int64_t* n_pairs);
@@ -149,7 +151,8 @@ void launch_pores_emit(const float* sdf, Dims d, const uint32_t* bits, const uns
                        long long words, const float origin[3], const float spacing[3],
                        pnm_pore* out, long long cap, unsigned grid, cudaStream_t s);
 // SDF pass only (for extract_pores alone).
-Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st);
+Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st,
+                    bool all_ascent = false);
 
 // ---- network flow (pnm_flow.cu) ------------------------------------------------------------
 struct FlowInputs {

@@ -57,6 +57,7 @@ __device__ __forceinline__ void push_edge(EdgeStage& st, const EdgeBuf& eb, unsi
   }
 }
 
+template <bool ALL_ASCENT>
 __global__ void __launch_bounds__(TX* TY)
     k_sdf_pass(const float* __restrict__ sdf, Dims d, float thr, uint8_t* __restrict__ code,
                int* __restrict__ nxt, int* __restrict__ L, uint32_t* __restrict__ peakbits,
@@ -74,13 +75,15 @@ __global__ void __launch_bounds__(TX* TY)
   if (t < HX) wx[t] = ((X0 - 1 + t) % nx + nx) % nx;
   if (t < HY) wy[t] = ((Y0 - 1 + t) % ny + ny) % ny;
   if (t < HZ) wz[t] = ((Z0 - 1 + t) % nz + nz) % nz;
+  const int lane = t & 31;  // == tx (TX == 32)
   __syncthreads();
-  for (int i = t; i < HX * HY * HZ; i += NT) {
-    const int hx = i % HX, hy = (i / HX) % HY, hz = i / (HX * HY);
-    s[hz][hy][hx] = __ldg(&sdf[wz[hz] * nxy + wy[hy] * nx + wx[hx]]);
+  for (int r = t >> 5; r < HY * HZ; r += NT / 32) {  // one halo row per warp iteration
+    const int hy = r % HY, hz = r / HY;
+    const float* src = sdf + (wz[hz] * nxy + wy[hy] * nx);
+    s[hz][hy][lane] = __ldg(&src[wx[lane]]);
+    if (lane < HX - 32) s[hz][hy][32 + lane] = __ldg(&src[wx[32 + lane]]);
   }
   __syncthreads();
-  const int lane = t & 31;  // == tx (TX == 32)
   const int tx = t % TX, ty = t / TX;
   const int gx = X0 + tx, gy = Y0 + ty;
   const bool inxy = gx < nx && gy < ny;
@@ -92,9 +95,14 @@ __global__ void __launch_bounds__(TX* TY)
     if (valid) {
       const float* c0 = &s[tz + 1][ty + 1][tx + 1];
       const float cv = *c0;
-      float bv = cv;
+      const int cls = cv > 0.0f ? CLS_PORE
+                                : (cv < thr ? CLS_MARKER : (!(cv >= 0.0f) ? CLS_FLOOD : CLS_ZERO));
       int bk = kSelf;
-      bool mk_nb = false, tie = false;
+      // ascent pointer: needed for every voxel by the flow basins, otherwise only where the
+      // gradient walk can start (sdf > 0) or a peak can sit (!(sdf <= 0), NaN included)
+      if (ALL_ASCENT || !(cv <= 0.0f)) {
+      float bv = cv;
+      bool tie = false;
       // fast scan with strict comparisons; any equality with the running maximum sends the voxel
       // through the exact tie-aware scan below (identical result whenever no tie occurs)
 #pragma unroll
@@ -107,7 +115,6 @@ __global__ void __launch_bounds__(TX* TY)
           bv = nv;
           bk = k;
         }
-        mk_nb |= (nv < thr);
       }
       if (tie) {
         bv = cv;
@@ -129,12 +136,22 @@ __global__ void __launch_bounds__(TX* TY)
           }
         }
       }
-      const int cls = cv > 0.0f ? CLS_PORE
-                                : (cv < thr ? CLS_MARKER : (!(cv >= 0.0f) ? CLS_FLOOD : CLS_ZERO));
-      code[ci] = make_code(bk, cls, cls == CLS_FLOOD && mk_nb);
       nxt[ci] = bk == kSelf ? ci
                             : wz[tz + bk / 9] * nxy + wy[ty + (bk / 3) % 3] * nx + wx[tx + bk % 3];
       if (!(cv <= 0.0f) && bk == kSelf) atomicOr(&peakbits[ci >> 5], 1u << (ci & 31));
+      }
+      // flood seed: a shallow-solid voxel with a marker neighbour (NaN is never < thr)
+      bool seed = false;
+      if (cls == CLS_FLOOD) {
+        float vmin = c0[-(HY * HX) - HX - 1];
+#pragma unroll
+        for (int k = 1; k < 27; ++k) {
+          if (k == kSelf) continue;
+          vmin = fminf(vmin, c0[(k / 9 - 1) * (HY * HX) + ((k / 3) % 3 - 1) * HX + (k % 3 - 1)]);
+        }
+        seed = vmin < thr;
+      }
+      code[ci] = make_code(bk, cls, seed);
       marker = cls == CLS_MARKER;
     }
     // run heads inside the chunk
@@ -519,20 +536,38 @@ __device__ __forceinline__ void hash_insert(unsigned long long* table, uint64_t 
   atomicOr(err, ERRF_HASH_FULL);
 }
 
-struct KeyLabels {  // label of voxel v from key[] and the id table in L[]
+// Label of voxel v for a warp whose lanes hold consecutive voxels of one row: from key[] and
+// the id table in L[] — lanes repeating the previous lane's key take the label from the first
+// lane of their run instead of gathering it again — or straight from a seg array.
+struct KeyLabels {
   const int* key;
   const int* L;
-  __device__ int operator()(int v) const { return label_of_key(L, __ldg(&key[v])); }
+  __device__ int operator()(int v, bool active) const {
+    const int k = active ? __ldg(&key[v]) : KEY_NONE;
+    const unsigned lane = threadIdx.x & 31;
+    const int pk = __shfl_up_sync(0xffffffffu, k, 1);
+    const bool lead = lane == 0 || pk != k;
+    const unsigned leaders = __ballot_sync(0xffffffffu, lead);
+    int lab = 0;
+    if (lead && active) lab = label_of_key(L, k);
+    const int src = 31 - __clz(leaders & (lane == 31 ? 0xffffffffu : ((2u << lane) - 1u)));
+    return __shfl_sync(0xffffffffu, lab, src);
+  }
 };
-struct SegLabels {  // label of voxel v from a seg array
+struct SegLabels {
   const int* seg;
-  __device__ int operator()(int v) const { return __ldg(&seg[v]); }
+  __device__ int operator()(int v, bool active) const { return active ? __ldg(&seg[v]) : 0; }
 };
 
 // One pass over 32 x 8 x 16 bricks (a warp owns a 32-voxel x-row and walks 16 z-planes): seg[v]
 // (optional) and every differing (+x,+y,+z) periodic face pair into the hash set. The +x label
 // comes from the neighbouring lane, the +z label is carried to the next plane. Lanes proposing
 // the pair of the previous lane skip their insert; lab_min/lab_max track the label range.
+__device__ __forceinline__ int lab_one(const KeyLabels& l, int v) {
+  return label_of_key(l.L, __ldg(&l.key[v]));
+}
+__device__ __forceinline__ int lab_one(const SegLabels& l, int v) { return __ldg(&l.seg[v]); }
+
 constexpr int STX = 32, STY = 8, STZ = 16;
 template <class Lab>
 __global__ void __launch_bounds__(STX* STY)
@@ -548,21 +583,19 @@ __global__ void __launch_bounds__(STX* STY)
   const int yp = y + 1 >= ny ? 0 : y + 1;
   const int nxy = nx * ny;
   int lmin = INT_MAX, lmax = INT_MIN;
-  int cur = in ? lab(z0 * nxy + y * nx + x) : 0;
+  if (y >= ny) return;  // warp-uniform: a warp is one row
+  int cur = lab(z0 * nxy + y * nx + x, in);
   for (int z = z0; z < z1; ++z) {
     const int row = z * nxy + y * nx;
     const int s0 = cur;
     if (seg && in) seg[row + x] = s0;
     const int zn = z + 1 >= nz ? 0 : z + 1;
     int sz = 0;
-    if (in && (want_pairs || z + 1 < z1)) sz = lab(zn * nxy + y * nx + x);
+    if (want_pairs || z + 1 < z1) sz = lab(zn * nxy + y * nx + x, in);
     if (want_pairs) {
       int sx = __shfl_down_sync(0xffffffffu, s0, 1);
-      int sy = 0;
-      if (in) {
-        if (lane == 31 || x + 1 >= nx) sx = lab(row + xp);
-        sy = lab(z * nxy + yp * nx + x);
-      }
+      const int sy = lab(z * nxy + yp * nx + x, in);
+      if (in && (lane == 31 || x + 1 >= nx)) sx = lab_one(lab, row + xp);
 #pragma unroll
       for (int dd = 0; dd < 3; ++dd) {
         const int s1 = dd == 0 ? sx : (dd == 1 ? sy : sz);
@@ -711,7 +744,8 @@ inline float marker_threshold(const float spacing[3]) {
 }
 }  // namespace
 
-Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st) {
+Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st,
+                    bool all_ascent) {
   const long long n = d.n();
   PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_EDGES], 0, sizeof(unsigned), c.stream));
   const long long words = (n + 31) / 32;
@@ -728,20 +762,26 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
   st->edges = eb.e;
   st->edge_cap = eb.cap;
   PNM_TRY(c.buf(S_NXT, n, &st->nxt));
-  k_sdf_pass<<<tile_grid(d), TX * TY, 0, c.stream>>>(d_sdf, d, marker_threshold(spacing),
-                                                     st->code, st->nxt, L, st->peakbits, eb,
-                                                     c.d_cnt); ++c.launches;
+  if (all_ascent)
+    k_sdf_pass<true><<<tile_grid(d), TX * TY, 0, c.stream>>>(d_sdf, d, marker_threshold(spacing),
+                                                           st->code, st->nxt, L, st->peakbits, eb,
+                                                           c.d_cnt);
+  else
+    k_sdf_pass<false><<<tile_grid(d), TX * TY, 0, c.stream>>>(d_sdf, d, marker_threshold(spacing),
+                                                            st->code, st->nxt, L, st->peakbits,
+                                                            eb, c.d_cnt); ++c.launches;
   PNM_CUDA(cudaGetLastError());
   st->idtab = L;
   return Status::ok();
 }
 
-Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st) {
+Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st,
+                        bool all_ascent) {
   const long long n = d.n();
   const long long words = (n + 31) / 32;
   cudaStream_t s = c.stream;
   PNM_CUDA(cudaMemsetAsync(c.d_cnt, 0, CNT_COUNT * sizeof(unsigned), s));
-  PNM_TRY(run_sdf_pass(c, d_sdf, d, spacing, st));
+  PNM_TRY(run_sdf_pass(c, d_sdf, d, spacing, st, all_ascent));
   int* L = st->idtab;
   int *key, *keylist, *f0, *f1, *tmp, *ulist;
   PNM_TRY(c.buf(S_ULIST, n, &ulist));
