@@ -62,7 +62,7 @@ enum Slot : int {
   // network flow
   S_U, S_V, S_W, S_P, S_OX, S_OY, S_OZ, S_FLOWLAB, S_FBITS, S_FCORE, S_FPREF, S_FID, S_FPAIR,
   S_FPAR, S_FFILM, S_FMINCORE, S_FLABEL, S_ROOTFLAG, S_SLOTOF, S_PEAK, S_NPORES_OUT,
-  S_PPRES, S_REC, S_ACC, S_TDP, S_THROATS, S_MAXBITS, S_FLOWOUT, S_ULIST, S_EDGES, S_NXT,
+  S_PPRES, S_REC, S_ACC, S_TDP, S_THROATS, S_MAXBITS, S_FLOWOUT, S_ULIST, S_EDGES, S_NXT, S_STEPS,
   S_COUNT
 };
 
@@ -121,7 +121,8 @@ struct SegState {
   Dims d;
   const float* sdf = nullptr;
   uint8_t* code = nullptr;      // per voxel: ascent direction (5 bits), class (2), flood-seed (1)
-  int32_t* nxt = nullptr;       // per voxel: ascent pointer (voxel id; itself at a local max)
+  int32_t* nxt = nullptr;       // per voxel: ascent jump target (voxel id; itself at a local max)
+  uint8_t* steps = nullptr;     // per voxel: ascent moves the jump covers (0 at a local max)
   int32_t* key = nullptr;       // per voxel: basin root (>=0), ~solid label (<0), INT_MIN none
   int32_t* idtab = nullptr;     // per key voxel: final signed label id
   uint32_t* peakbits = nullptr; // bitmap of extract_pores peaks
