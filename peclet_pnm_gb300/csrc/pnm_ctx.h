@@ -121,8 +121,7 @@ struct SegState {
   Dims d;
   const float* sdf = nullptr;
   uint8_t* code = nullptr;      // per voxel: ascent direction (5 bits), class (2), flood-seed (1)
-  int32_t* nxt = nullptr;       // per voxel: ascent jump target (voxel id; itself at a local max)
-  uint8_t* steps = nullptr;     // per voxel: ascent moves the jump covers (0 at a local max)
+  int32_t* nxt = nullptr;       // per voxel: ascent pointer (voxel id; itself at a local max)
   int32_t* key = nullptr;       // per voxel: basin root (>=0), ~solid label (<0), INT_MIN none
   int32_t* idtab = nullptr;     // per key voxel: final signed label id
   uint32_t* peakbits = nullptr; // bitmap of extract_pores peaks

@@ -109,31 +109,14 @@ __device__ __forceinline__ void uf_unite_s(int* L, int a, int b) {
   }
 }
 
-// nxt[v] is the voxel `steps[v]` ascent moves ahead of v (steps 0: v is a fixed point); a jump
-// that would overshoot the 512-move budget is replaced by single moves along the direction bits.
-__device__ __forceinline__ int chase_root(const int* __restrict__ nxt,
-                                          const uint8_t* __restrict__ steps,
-                                          const uint8_t* __restrict__ code, int v, Dims d) {
-  int cur = v, moved = 0;
-  while (moved < 512) {
-    const int s = __ldg(&steps[cur]);
-    if (s == 0) break;
-    if (moved + s <= 512) {
-      moved += s;
-      cur = __ldg(&nxt[cur]);
-      continue;
-    }
-    const int nx = d.nx, ny = d.ny, nz = d.nz;  // rare: finish move by move
-    int x = cur % nx, y = (cur / nx) % ny, z = cur / (nx * ny);
-    while (moved < 512) {
-      const int dir = code_dir(__ldg(&code[cur]));
-      if (dir == kSelf) break;
-      x = wrap1(x + dir % 3 - 1, nx);
-      y = wrap1(y + (dir / 3) % 3 - 1, ny);
-      z = wrap1(z + dir / 9 - 1, nz);
-      cur = (z * ny + y) * nx + x;
-      ++moved;
-    }
+// Gradient root: follow the ascent pointers (nxt, a voxel id; a local max points at itself) for
+// at most 512 moves (pore_extraction.hpp:277-309 and :626-648; MAX_STEPS = 512).
+__device__ __forceinline__ int chase_root(const int* __restrict__ nxt, int v) {
+  int cur = v;
+  for (int s = 0; s < 512; ++s) {
+    const int n2 = __ldg(&nxt[cur]);
+    if (n2 == cur) break;
+    cur = n2;
   }
   return cur;
 }

@@ -229,13 +229,13 @@ __global__ void k_centers_pressure(const float* __restrict__ sdf, Dims d, Geo g,
 // already carry their root in key[]; other cells chase the ascent pointers.
 __global__ void __launch_bounds__(256)
     k_flow_basins(Dims d, const uint8_t* __restrict__ code, const int* __restrict__ nxt,
-                  const uint8_t* __restrict__ steps, const int* __restrict__ key,
+                  const int* __restrict__ key,
                   const int* __restrict__ seg, int* __restrict__ flowLab) {
   const long long n = d.n();
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += (long long)gridDim.x * blockDim.x) {
     const uint8_t c0 = code[v];
-    const int root = code_cls(c0) == CLS_PORE ? key[v] : chase_root(nxt, steps, code, (int)v, d);
+    const int root = code_cls(c0) == CLS_PORE ? key[v] : chase_root(nxt, (int)v);
     flowLab[v] = __ldg(&seg[root]);
   }
 }
@@ -671,8 +671,7 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
   }
   k_centers_pressure<<<gridn(np, c.sm_count), 256, 0, s>>>(st.sdf, d, geo, peak, np, in.p, pores,
                                                            ppres); ++c.launches;
-  k_flow_basins<<<gridn(n, c.sm_count), 256, 0, s>>>(d, st.code, st.nxt, st.steps, st.key, seg,
-                                                      flowLab); ++c.launches;
+  k_flow_basins<<<gridn(n, c.sm_count), 256, 0, s>>>(d, st.code, st.nxt, st.key, seg, flowLab); ++c.launches;
   PNM_CUDA(cudaGetLastError());
 
   // face classification + bounds

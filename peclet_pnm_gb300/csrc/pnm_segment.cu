@@ -27,50 +27,43 @@ constexpr int kBig = INT_MAX;           // unset min-index / non-marker parent
 //  * ascent direction = lexicographic max of (sdf, wrapped index) over the voxel and its 26
 //    neighbours, scanned dz->dy->dx with the reference's comparisons (pore_extraction.hpp:284-304,
 //    :632-644); it points at the voxel itself exactly when the voxel is a strict local max
-//    (:93-104). Stored as direction bits of `code`, and followed inside the tile: nxt = the voxel
-//    where the ascent chain leaves the tile (or its fixed point, or after 255 moves), steps = the
-//    moves taken, so the global root chase needs few hops and still counts moves exactly;
+//    (:93-104). Stored as direction bits of `code` and as the neighbour's id in nxt;
 //  * class (marker :177, flood :245-248, pore :276), flood seed (has a marker neighbour), peak
 //    bit for extract_pores (:89-106): !(sdf <= 0) and the voxel is its own ascent target.
-// Marker CCL (:181-230), first half: a marker's run head is the first marker of its run inside
-// the chunk (runs are connected). Adjacency to the 13 forward neighbours (:204-206) links run
-// heads with runs of the four forward rows and across the chunk end; links inside the tile are
-// united in a shared-memory union-find, links leaving the tile are emitted as edges (local root,
-// neighbour) for k_ccl_edges. L = global id of the marker's tile-local root; kBig elsewhere.
+// Marker CCL (:181-230), first half: a marker's union-find parent is the first marker of its run
+// inside the chunk (runs are connected). Adjacency to the 13 forward neighbours (:204-206) is
+// emitted as edges (run head, head of a touching run of the four forward rows, or the voxel
+// across the chunk end); lanes drop links the previous lane already made, each warp reserves
+// its edges with one shared-memory atomic and each block with one global atomic.
 struct EdgeBuf {
   int2* e;
   unsigned cap;
 };
-constexpr int kCross = 1024;  // cross-tile edges staged per block; more spill straight to global
+constexpr int kStage = 2048;  // edges staged per block; a full stage spills straight to global
 
 template <bool ALL_ASCENT>
 __global__ void __launch_bounds__(TX* TY)
     k_sdf_pass(const float* __restrict__ sdf, Dims d, float thr, uint8_t* __restrict__ code,
-               int* __restrict__ nxt, uint8_t* __restrict__ steps, int* __restrict__ L,
-               uint32_t* __restrict__ peakbits, EdgeBuf eb, unsigned* cnt) {
-  constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2, NT = TX * TY, NV = TX * TY * TZ;
+               int* __restrict__ nxt, int* __restrict__ L, uint32_t* __restrict__ peakbits,
+               EdgeBuf eb, unsigned* cnt) {
+  constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2, NT = TX * TY;
   __shared__ float s[HZ][HY][HX];
   __shared__ int wx[HX], wy[HY], wz[HZ];
   __shared__ unsigned rowm[HZ][HY];       // markers of each halo row at x = X0 .. X0+31
   __shared__ unsigned char rowh[HZ][HY];  // bit 0: marker at x = X0-1; bit 1: at x = X0+32
-  __shared__ int par[NV];                 // tile-local union-find over run heads (local ids)
-  __shared__ short nl[NV];                // in-tile ascent successor (local id), -1: leaves tile
-  __shared__ unsigned char dirs[NV];      // ascent direction
-  __shared__ int2 cross[kCross];          // (local head, global neighbour) links leaving the tile
-  __shared__ unsigned ncross, gbase;
+  __shared__ int2 stage[kStage];
+  __shared__ unsigned nstage, gbase;
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int nxy = nx * ny;
   const int X0 = blockIdx.x * TX, Y0 = blockIdx.y * TY, Z0 = blockIdx.z * TZ;
-  const int TXe = min(TX, nx - X0), TYe = min(TY, ny - Y0), TZe = min(TZ, nz - Z0);
   const int t = threadIdx.x;
   const int lane = t & 31;  // == tx (TX == 32)
-  if (t == 0) ncross = 0;
+  if (t == 0) nstage = 0;
   if (t < HX) wx[t] = ((X0 - 1 + t) % nx + nx) % nx;
   if (t < HY) wy[t] = ((Y0 - 1 + t) % ny + ny) % ny;
   if (t < HZ) wz[t] = ((Z0 - 1 + t) % nz + nz) % nz;
   __syncthreads();
-  // A: halo rows; B: marker masks of every halo row
-  for (int r = t >> 5; r < HY * HZ; r += NT / 32) {
+  for (int r = t >> 5; r < HY * HZ; r += NT / 32) {  // halo rows and their marker masks
     const int hy = r % HY, hz = r / HY;
     const float* src = sdf + (wz[hz] * nxy + wy[hy] * nx);
     const float v0 = __ldg(&src[wx[lane + 1]]);
@@ -92,19 +85,16 @@ __global__ void __launch_bounds__(TX* TY)
   const int gx = X0 + tx, gy = Y0 + ty;
   const bool inxy = gx < nx && gy < ny;
   const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
-  // C: per voxel classification, ascent, seeds, peaks, run heads
   for (int tz = 0; tz < TZ; ++tz) {
     const int gz = Z0 + tz;
     const bool valid = inxy && gz < nz;
-    const int li = (tz * TY + ty) * TX + tx;
     const int ci = gz * nxy + gy * nx + gx;
-    int bk = kSelf;
-    short nlv = (short)li;
     if (valid) {
       const float* c0 = &s[tz + 1][ty + 1][tx + 1];
       const float cv = *c0;
       const int cls = cv > 0.0f ? CLS_PORE
                                 : (cv < thr ? CLS_MARKER : (!(cv >= 0.0f) ? CLS_FLOOD : CLS_ZERO));
+      int bk = kSelf;
       // ascent: every voxel for the flow basins, otherwise where a walk starts (sdf > 0) or a
       // peak can sit (!(sdf <= 0), NaN included)
       if (ALL_ASCENT || !(cv <= 0.0f)) {
@@ -141,12 +131,8 @@ __global__ void __launch_bounds__(TX* TY)
             }
           }
         }
-        if (bk != kSelf) {
-          const int lx = tx + bk % 3 - 1, ly = ty + (bk / 3) % 3 - 1, lz = tz + bk / 9 - 1;
-          nlv = (lx >= 0 && lx < TXe && ly >= 0 && ly < TYe && lz >= 0 && lz < TZe)
-                    ? (short)((lz * TY + ly) * TX + lx)
-                    : (short)-1;
-        }
+        nxt[ci] = bk == kSelf ? ci
+                              : wz[tz + bk / 9] * nxy + wy[ty + (bk / 3) % 3] * nx + wx[tx + bk % 3];
         if (!(cv <= 0.0f) && bk == kSelf) atomicOr(&peakbits[ci >> 5], 1u << (ci & 31));
       }
       bool seed = false;  // a shallow-solid voxel with a marker neighbour (NaN is never < thr)
@@ -161,170 +147,89 @@ __global__ void __launch_bounds__(TX* TY)
       }
       code[ci] = make_code(bk, cls, seed);
     }
-    dirs[li] = (unsigned char)bk;
-    nl[li] = nlv;
-    const unsigned m = valid ? rowm[tz + 1][ty + 1] : 0u;
-    if (valid && ((m >> lane) & 1u) && (lane == 0 || !((m >> (lane - 1)) & 1u))) par[li] = li;
-  }
-  __syncthreads();
-  // D: marker links (local unions / staged cross-tile edges) and in-tile ascent jumps
-  for (int tz = 0; tz < TZ; ++tz) {
-    const int gz = Z0 + tz;
-    const bool valid = inxy && gz < nz;
-    const int li = (tz * TY + ty) * TX + tx;
-    const int ci = gz * nxy + gy * nx + gx;
+    // marker runs of this chunk row
     const unsigned m = rowm[tz + 1][ty + 1];
     const bool marker = valid && ((m >> lane) & 1u);
     const int hl = marker ? 31 - __clz((m & ~(m << 1)) & upto) : 0;
-    const int hli = (tz * TY + ty) * TX + hl;  // local id of the run head
-    if (__any_sync(0xffffffffu, marker)) {
-      // chunk end: the +x neighbour lies in the next chunk (or wraps)
-      if (marker && (lane == 31 || gx + 1 == nx) && s[tz + 1][ty + 1][tx + 2] < thr) {
-        const int xr = wx[tx + 2];
-        if (xr - X0 >= 0 && xr - X0 < TXe) {  // wraps into this chunk
-          const int p = xr - X0;
-          const int hp = 31 - __clz((m & ~(m << 1)) & (p == 31 ? 0xffffffffu : ((2u << p) - 1u)));
-          uf_unite_s(par, hli, (tz * TY + ty) * TX + hp);
+    const int head = gz * nxy + gy * nx + X0 + hl;
+    if (valid) L[ci] = marker ? head : kBig;
+    if (!__any_sync(0xffffffffu, marker)) continue;
+    // links: up to two touching runs per forward row plus the +x voxel across the chunk end
+    int rep[9];
+    unsigned have = 0;
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {  // forward rows (dy,dz) = (1,0), (-1,1), (0,1), (1,1)
+      const int sy = ty + 1 + ((f == 0 || f == 3) ? 1 : (f == 1 ? -1 : 0));
+      const int sz = tz + 1 + (f == 0 ? 0 : 1);
+      const unsigned m2 = rowm[sz][sy];
+      const unsigned hb = rowh[sz][sy];
+      const unsigned st2 = m2 & ~(m2 << 1);
+      int c0 = -2, c1 = -2;  // chunk positions; -1 / 32: the halo columns
+      if (marker) {
+        if ((m2 >> lane) & 1u) {
+          c0 = 31 - __clz(st2 & upto);
         } else {
-          const unsigned q = atomicAdd(&ncross, 1u);
-          const int2 e = make_int2(hli, gz * nxy + gy * nx + xr);
-          if (q < (unsigned)kCross) cross[q] = e;
-          else {
-            const unsigned g = atomicAdd(&cnt[CNT_EDGES], 1u);
-            if (g < eb.cap) eb.e[g] = make_int2(ci - lane + hl, e.y);
+          if (lane > 0) {
+            if ((m2 >> (lane - 1)) & 1u) c0 = 31 - __clz(st2 & (upto >> 1));
+          } else if (hb & 1u) {
+            c0 = -1;
+          }
+          if (lane < 31) {
+            if ((m2 >> (lane + 1)) & 1u) c1 = lane + 1;
+          } else if (hb & 2u) {
+            c1 = 32;
           }
         }
       }
-#pragma unroll
-      for (int f = 0; f < 4; ++f) {  // forward rows (dy,dz) = (1,0), (-1,1), (0,1), (1,1)
-        const int fdy = (f == 0 || f == 3) ? 1 : (f == 1 ? -1 : 0), fdz = f == 0 ? 0 : 1;
-        const int sy = ty + 1 + fdy, sz = tz + 1 + fdz;
-        const unsigned m2 = rowm[sz][sy];
-        const unsigned hb = rowh[sz][sy];
-        const unsigned st2 = m2 & ~(m2 << 1);
-        // neighbour runs touching x-1..x+1, as chunk positions (-1 / 32: halo columns)
-        int c0 = -2, c1 = -2;
-        if (marker) {
-          if ((m2 >> lane) & 1u) {
-            c0 = 31 - __clz(st2 & upto);
-          } else {
-            if (lane > 0) {
-              if ((m2 >> (lane - 1)) & 1u) c0 = 31 - __clz(st2 & (upto >> 1));
-            } else if (hb & 1u) {
-              c0 = -1;
-            }
-            if (lane < 31) {
-              if ((m2 >> (lane + 1)) & 1u) c1 = lane + 1;
-            } else if (hb & 2u) {
-              c1 = 32;
-            }
-          }
-        }
-        // lanes of one run repeat the previous lane's links: keep the new ones
-        const int ph = __shfl_up_sync(0xffffffffu, hli, 1);
-        const int p0 = __shfl_up_sync(0xffffffffu, c0, 1);
-        const int p1 = __shfl_up_sync(0xffffffffu, c1, 1);
-        const bool same = lane > 0 && ph == hli;
-        const int ly = ty + fdy, lz = tz + fdz;
-        const bool row_in = ly >= 0 && ly < TYe && lz < TZe;
-        const int rowg = wz[sz] * nxy + wy[sy] * nx;
-#pragma unroll
-        for (int j = 0; j < 2; ++j) {
-          const int c = j == 0 ? c0 : c1;
-          if (c == -2 || (same && (c == p0 || c == p1))) continue;
-          if (row_in && c >= 0 && c < TXe) {
-            uf_unite_s(par, hli, (lz * TY + ly) * TX + c);
-          } else {
-            const int rep = rowg + wx[c + 1];
-            const unsigned q = atomicAdd(&ncross, 1u);
-            if (q < (unsigned)kCross) {
-              cross[q] = make_int2(hli, rep);
-            } else {
-              const unsigned g = atomicAdd(&cnt[CNT_EDGES], 1u);
-              if (g < eb.cap) eb.e[g] = make_int2(ci - lane + hl, rep);
-            }
-          }
-        }
+      const int p0 = __shfl_up_sync(0xffffffffu, c0, 1);
+      const int p1 = __shfl_up_sync(0xffffffffu, c1, 1);
+      const int ph = __shfl_up_sync(0xffffffffu, head, 1);
+      const bool same = lane > 0 && ph == head;
+      const int rowg = wz[sz] * nxy + wy[sy] * nx;
+      if (c0 != -2 && !(same && (c0 == p0 || c0 == p1))) {
+        rep[2 * f] = rowg + wx[c0 + 1];
+        have |= 1u << (2 * f);
+      }
+      if (c1 != -2 && !(same && (c1 == p0 || c1 == p1))) {
+        rep[2 * f + 1] = rowg + wx[c1 + 1];
+        have |= 1u << (2 * f + 1);
       }
     }
-    // in-tile ascent jump (for every voxel whose ascent was computed)
-    if (valid && (ALL_ASCENT || !(s[tz + 1][ty + 1][tx + 1] <= 0.0f))) {
-      int cur = li, n_st = 0;
-      int jump = ci;
-      while (true) {
-        const int nn = nl[cur];
-        if (nn == cur) {  // fixed point
-          jump = (Z0 + cur / (TX * TY)) * nxy + (Y0 + (cur / TX) % TY) * nx + X0 + cur % TX;
-          break;
-        }
-        if (nn < 0) {  // the next move leaves the tile
-          const int k = dirs[cur];
-          const int cx = cur % TX, cy = (cur / TX) % TY, cz = cur / (TX * TY);
-          jump = wz[cz + k / 9] * nxy + wy[cy + (k / 3) % 3] * nx + wx[cx + k % 3];
-          ++n_st;
-          break;
-        }
-        cur = nn;
-        if (++n_st == 255) {
-          jump = (Z0 + cur / (TX * TY)) * nxy + (Y0 + (cur / TX) % TY) * nx + X0 + cur % TX;
-          break;
-        }
-      }
-      nxt[ci] = jump;
-      steps[ci] = (uint8_t)n_st;
+    if (marker && (lane == 31 || gx + 1 == nx) && s[tz + 1][ty + 1][tx + 2] < thr) {
+      rep[8] = gz * nxy + gy * nx + wx[tx + 2];
+      have |= 1u << 8;
     }
-  }
-  __syncthreads();
-  // E: flatten the tile-local forest (read-only walks, then one store each), publish L
-  int roots[TZ];
+    // warp-compacted staging: one shared-memory reservation per warp
+    const unsigned mine = __popc(have);
+    unsigned incl = mine;
 #pragma unroll
-  for (int tz = 0; tz < TZ; ++tz) {
-    const int li = (tz * TY + ty) * TX + tx;
-    const unsigned m = rowm[tz + 1][ty + 1];
-    const bool head = inxy && Z0 + tz < nz && ((m >> lane) & 1u) &&
-                      !(lane > 0 && ((m >> (lane - 1)) & 1u));
-    int r = li;
-    if (head) {
-      for (int it = 0; it < NV; ++it) {
-        const int p = par[r];
-        if (p == r) break;
-        r = p;
-      }
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
     }
-    roots[tz] = r;
-  }
-  __syncthreads();
+    const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+    unsigned base = 0;
+    if (lane == 0 && total) base = atomicAdd(&nstage, total);
+    base = __shfl_sync(0xffffffffu, base, 0) + incl - mine;
 #pragma unroll
-  for (int tz = 0; tz < TZ; ++tz) {
-    const int li = (tz * TY + ty) * TX + tx;
-    const unsigned m = rowm[tz + 1][ty + 1];
-    const bool head = inxy && Z0 + tz < nz && ((m >> lane) & 1u) &&
-                      !(lane > 0 && ((m >> (lane - 1)) & 1u));
-    if (head) par[li] = roots[tz];
-  }
-  __syncthreads();
-  auto gid = [&](int l) {
-    return (Z0 + l / (TX * TY)) * nxy + (Y0 + (l / TX) % TY) * nx + X0 + l % TX;
-  };
-  for (int tz = 0; tz < TZ; ++tz) {
-    const int gz = Z0 + tz;
-    if (!inxy || gz >= nz) continue;
-    const unsigned m = rowm[tz + 1][ty + 1];
-    const int ci = gz * nxy + gy * nx + gx;
-    int out = kBig;
-    if ((m >> lane) & 1u) {
-      const int hl = 31 - __clz((m & ~(m << 1)) & upto);
-      out = gid(par[(tz * TY + ty) * TX + hl]);
+    for (int j = 0; j < 9; ++j) {
+      if (!((have >> j) & 1u)) continue;
+      const int2 e = make_int2(head, rep[j]);
+      if (base < (unsigned)kStage) {
+        stage[base] = e;
+      } else {
+        const unsigned g = atomicAdd(&cnt[CNT_EDGES], 1u);
+        if (g < eb.cap) eb.e[g] = e;
+      }
+      ++base;
     }
-    L[ci] = out;
   }
-  const unsigned nc = min(ncross, (unsigned)kCross);
-  if (t == 0) gbase = nc ? atomicAdd(&cnt[CNT_EDGES], nc) : 0u;
   __syncthreads();
-  for (unsigned i = t; i < nc; i += NT) {
-    const int2 e = cross[i];
-    if (gbase + i < eb.cap) eb.e[gbase + i] = make_int2(gid(par[e.x]), e.y);
-  }
+  const unsigned ns = min(nstage, (unsigned)kStage);
+  if (t == 0) gbase = ns ? atomicAdd(&cnt[CNT_EDGES], ns) : 0u;
+  __syncthreads();
+  for (unsigned i = t; i < ns; i += NT)
+    if (gbase + i < eb.cap) eb.e[gbase + i] = stage[i];
 }
 
 // ---- 2. marker CCL, second half ------------------------------------------------------------
@@ -380,9 +285,8 @@ __global__ void __launch_bounds__(256) k_ccl_all(Dims d, int* L, unsigned* err) 
 // (flood labels follow in k_flood_seed). Lanes of a warp whose markers share a union-find parent
 // run one find for the group.
 __global__ void __launch_bounds__(256)
-    k_resolve(Dims d, const uint8_t* __restrict__ code, const int* __restrict__ nxt,
-              const uint8_t* __restrict__ steps, int* L, int* __restrict__ key,
-              int* __restrict__ keylist, unsigned* cnt) {
+    k_resolve(Dims d, const uint8_t* __restrict__ code, const int* __restrict__ nxt, int* L,
+              int* __restrict__ key, int* __restrict__ keylist, unsigned* cnt) {
   const long long n = d.n();
   unsigned* err = &cnt[CNT_ERR];
   for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
@@ -398,7 +302,7 @@ __global__ void __launch_bounds__(256)
       if (cls == CLS_MARKER) {
         par = ld_relaxed(&L[v]);
       } else if (cls == CLS_PORE) {
-        const int r = chase_root(nxt, steps, code, v, d);
+        const int r = chase_root(nxt, v);
         k = r;
         agg = r;
       }
@@ -876,15 +780,14 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
   st->edges = eb.e;
   st->edge_cap = eb.cap;
   PNM_TRY(c.buf(S_NXT, n, &st->nxt));
-  PNM_TRY(c.buf(S_STEPS, n, &st->steps));
   if (all_ascent)
     k_sdf_pass<true><<<tile_grid(d), TX * TY, 0, c.stream>>>(d_sdf, d, marker_threshold(spacing),
-                                                           st->code, st->nxt, st->steps, L,
-                                                           st->peakbits, eb, c.d_cnt);
+                                                           st->code, st->nxt, L, st->peakbits,
+                                                           eb, c.d_cnt);
   else
     k_sdf_pass<false><<<tile_grid(d), TX * TY, 0, c.stream>>>(d_sdf, d, marker_threshold(spacing),
-                                                            st->code, st->nxt, st->steps, L,
-                                                            st->peakbits, eb, c.d_cnt); ++c.launches;
+                                                            st->code, st->nxt, L, st->peakbits,
+                                                            eb, c.d_cnt); ++c.launches;
   PNM_CUDA(cudaGetLastError());
   st->idtab = L;
   return Status::ok();
@@ -918,8 +821,8 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
     PNM_CUDA(cudaGetLastError());
   }
   st->n_edges = n_edges;
-  k_resolve<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, st->code, st->nxt, st->steps, L, key,
-                                                          keylist, c.d_cnt); ++c.launches;
+  k_resolve<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, st->code, st->nxt, L, key, keylist,
+                                                          c.d_cnt); ++c.launches;
   PNM_CUDA(cudaGetLastError());
   k_flood_seed<<<tile_grid(d), TX * TY, 0, s>>>(d, st->code, key, L, ulist, c.d_cnt); ++c.launches;
   const unsigned fgrid = grid_for(n, 256, c.sm_count, 4);
