@@ -274,6 +274,28 @@ __global__ void __launch_bounds__(256) k_ccl_all(Dims d, int* L, unsigned* err) 
   }
 }
 
+// ---- pointer doubling of the ascent pointers: out = in o in, for the voxels whose pointer the
+// pipeline reads (every voxel when all_ascent, else those with !(sdf <= 0), i.e. pore-or-NaN
+// class bits with a computed direction). Two passes turn nxt into nxt4.
+template <bool ALL>
+__global__ void __launch_bounds__(256)
+    k_nxt_double(Dims d, const uint8_t* __restrict__ code, const int* __restrict__ in,
+                 int* __restrict__ out) {
+  const long long n = d.n();
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (long long)gridDim.x * blockDim.x) {
+    if (!ALL) {
+      const int cls = code_cls(code[v]);
+      if (cls != CLS_PORE && cls != CLS_FLOOD) continue;  // FLOOD covers NaN (sdf unordered)
+      if (cls == CLS_FLOOD && code_dir(code[v]) == kSelf) {
+        out[v] = (int)v;  // NaN or a shallow-solid voxel without a computed pointer
+        continue;
+      }
+    }
+    out[v] = __ldg(&in[__ldg(&in[v])]);
+  }
+}
+
 // ---- 3. resolve ----------------------------------------------------------------------------------
 // Gradient root of a voxel: follow the ascent pointers for at most 512 moves
 // (pore_extraction.hpp:277-309 and :626-648; MAX_STEPS = 512).
@@ -821,6 +843,19 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
     PNM_CUDA(cudaGetLastError());
   }
   st->n_edges = n_edges;
+  {  // nxt -> nxt4 (the second buffer is the flood's tmp list, unused until the flood)
+    int* nxt2 = nullptr;
+    PNM_TRY(c.buf(S_TMP, n, &nxt2));
+    const unsigned g = grid_for(n, 256, c.sm_count);
+    if (all_ascent) {
+      k_nxt_double<true><<<g, 256, 0, s>>>(d, st->code, st->nxt, nxt2);
+      k_nxt_double<true><<<g, 256, 0, s>>>(d, st->code, nxt2, st->nxt);
+    } else {
+      k_nxt_double<false><<<g, 256, 0, s>>>(d, st->code, st->nxt, nxt2);
+      k_nxt_double<false><<<g, 256, 0, s>>>(d, st->code, nxt2, st->nxt);
+    }
+    c.launches += 2;
+  }
   k_resolve<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, st->code, st->nxt, L, key, keylist,
                                                           c.d_cnt); ++c.launches;
   PNM_CUDA(cudaGetLastError());
