@@ -364,39 +364,38 @@ __global__ void __launch_bounds__(256)
 // (layer 2) and from each previous layer (t >= 3). Discovery marks a layer PENDING, assignment
 // computes its labels into `tmp`, and the next discovery publishes them, so no voxel ever sees a
 // same-sweep label — exactly the double-buffered Jacobi sweep.
-__device__ __forceinline__ unsigned block_append(unsigned* cnt, bool take, unsigned* sh_base) {
-  // one global reservation per block: exclusive rank of `take` across the block
-  unsigned tot;
-  const unsigned r = block_exclusive_sum(take ? 1u : 0u, &tot);
-  if (threadIdx.x == 0) *sh_base = tot ? atomicAdd(cnt, tot) : 0u;
-  __syncthreads();
-  const unsigned b = *sh_base;
-  __syncthreads();
-  return b + r;
-}
-
 __global__ void __launch_bounds__(TX* TY)
     k_flood_seed(Dims d, const uint8_t* __restrict__ code, int* __restrict__ key, int* L,
                  int* __restrict__ ulist, unsigned* cnt) {
   constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2, NT = TX * TY;
   __shared__ int mk[HZ][HY][HX];  // marker neighbours' keys (~root), INT_MIN elsewhere
   __shared__ int wx[HX], wy[HY], wz[HZ];
-  __shared__ unsigned sh_base;
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int nxy = nx * ny;
   const int X0 = blockIdx.x * TX, Y0 = blockIdx.y * TY, Z0 = blockIdx.z * TZ;
   const int t = threadIdx.x;
+  const int lane = t & 31;
   if (t < HX) wx[t] = ((X0 - 1 + t) % nx + nx) % nx;
   if (t < HY) wy[t] = ((Y0 - 1 + t) % ny + ny) % ny;
   if (t < HZ) wz[t] = ((Z0 - 1 + t) % nz + nz) % nz;
   __syncthreads();
-  for (int i = t; i < HX * HY * HZ; i += NT) {
-    const int hx = i % HX, hy = (i / HX) % HY, hz = i / (HX * HY);
-    const int g = wz[hz] * nxy + wy[hy] * nx + wx[hx];
-    (&mk[0][0][0])[i] = code_cls(__ldg(&code[g])) == CLS_MARKER ? __ldg(&key[g]) : INT_MIN;
+  for (int r = t >> 5; r < HY * HZ; r += NT / 32) {  // one halo row per warp iteration
+    const int hy = r % HY, hz = r / HY;
+    const int rb = wz[hz] * nxy + wy[hy] * nx;
+    const int g0 = rb + wx[lane + 1];
+    const uint8_t c0 = __ldg(&code[g0]);
+    const int k0 = __ldg(&key[g0]);  // independent of the code load
+    mk[hz][hy][lane + 1] = code_cls(c0) == CLS_MARKER ? k0 : INT_MIN;
+    if (lane < 2) {
+      const int hx = lane == 0 ? 0 : HX - 1;
+      const int g1 = rb + wx[hx];
+      const uint8_t c1 = __ldg(&code[g1]);
+      const int k1 = __ldg(&key[g1]);
+      mk[hz][hy][hx] = code_cls(c1) == CLS_MARKER ? k1 : INT_MIN;
+    }
   }
   __syncthreads();
-  const int tx = t % TX, ty = t / TX;
+  const int tx = lane, ty = t >> 5;
   const int gx = X0 + tx, gy = Y0 + ty;
   for (int tz = 0; tz < TZ; ++tz) {
     const int gz = Z0 + tz;
@@ -422,7 +421,7 @@ __global__ void __launch_bounds__(TX* TY)
         }
       }
     }
-    const unsigned pos = block_append(&cnt[CNT_FRONT_SPARE], rest, &sh_base);
+    const int pos = warp_append(&cnt[CNT_FRONT_SPARE], rest);
     if (rest) ulist[pos] = ci;
   }
 }
