@@ -57,6 +57,13 @@ def edge_cases():
     s[2:4, 2::4, :35] = 2.0
     s[1:5, 0:3, 0:3] = -4.0
     out.append(("deep_flood_serpentine", s, *UNIT))
+    # adversarial marker patterns for the CCL edge lists: runs of length one everywhere
+    zz, yy, xx = np.meshgrid(np.arange(20), np.arange(18), np.arange(40), indexing="ij")
+    chk = np.where((xx + yy + zz) % 2 == 0, -3.0, 0.75).astype(np.float32)
+    out.append(("checker_markers", chk, *UNIT))
+    rm = np.where(rng.random((24, 20, 70)) < 0.5, -3.0, 1.0).astype(np.float32)
+    rm += rng.uniform(0, 0.01, size=rm.shape).astype(np.float32)
+    out.append(("random_markers", rm, *UNIT))
     # random noise (many tiny components) with anisotropic spacing and an origin
     out.append(("noise_16_aniso", rng.normal(0.0, 1.5, size=(16, 17, 18)).astype(np.float32),
                 [0.25, -3.0, 7.5], [0.7, 1.3, 2.1]))
