@@ -109,13 +109,12 @@ __device__ __forceinline__ void uf_unite_s(int* L, int a, int b) {
   }
 }
 
-// Gradient root: the voxel reached after at most 512 ascent moves (pore_extraction.hpp:277-309
-// and :626-648; MAX_STEPS = 512). nxt4 is the ascent pointer composed four times (a local max
-// points at itself and absorbs), so 128 hops of nxt4 are exactly 512 moves.
-__device__ __forceinline__ int chase_root(const int* __restrict__ nxt4, int v) {
+// Gradient root: follow the ascent pointers (nxt, a voxel id; a local max points at itself) for
+// at most 512 moves (pore_extraction.hpp:277-309 and :626-648; MAX_STEPS = 512).
+__device__ __forceinline__ int chase_root(const int* __restrict__ nxt, int v) {
   int cur = v;
-  for (int h = 0; h < 128; ++h) {
-    const int n2 = __ldg(&nxt4[cur]);
+  for (int s = 0; s < 512; ++s) {
+    const int n2 = __ldg(&nxt[cur]);
     if (n2 == cur) break;
     cur = n2;
   }

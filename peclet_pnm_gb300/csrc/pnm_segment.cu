@@ -23,21 +23,18 @@ constexpr int kBig = INT_MAX;           // unset min-index / non-marker parent
 
 // ---- 1. SDF pass ---------------------------------------------------------------------------
 // A 32x8x8 tile in shared memory with a one-voxel periodic halo; one warp = one 32-voxel x-row
-// chunk, each thread walks the 8 z-planes of its column with a 3x3x3 register window. Per voxel:
+// chunk, each thread walks the 8 z-planes of its column. Per voxel:
 //  * ascent direction = lexicographic max of (sdf, wrapped index) over the voxel and its 26
-//    neighbours (pore_extraction.hpp:284-304, :632-644). Away from the volume boundary the wrapped
-//    index grows with the neighbour number k (dz, dy, dx major to minor), so the reference's
-//    sequential scan equals "largest k whose value equals the maximum"; boundary voxels and NaN
-//    centres run the reference's comparison sequence itself. The direction is stored in `code`
-//    and as the neighbour's id in nxt; it points at the voxel exactly at a strict local max
-//    (:93-104);
+//    neighbours, scanned dz->dy->dx with the reference's comparisons (pore_extraction.hpp:284-304,
+//    :632-644); it points at the voxel itself exactly when the voxel is a strict local max
+//    (:93-104). Stored as direction bits of `code` and as the neighbour's id in nxt;
 //  * class (marker :177, flood :245-248, pore :276), flood seed (has a marker neighbour), peak
 //    bit for extract_pores (:89-106): !(sdf <= 0) and the voxel is its own ascent target.
 // Marker CCL (:181-230), first half: a marker's union-find parent is the first marker of its run
-// inside the chunk (runs are connected). Each run head lists the runs of the four forward rows
-// its dilated extent touches, and the voxel across the chunk end, as edges (the reference's 13
-// forward neighbours, :204-206); each warp reserves its edges with one shared-memory atomic and
-// each block with one global atomic.
+// inside the chunk (runs are connected). Adjacency to the 13 forward neighbours (:204-206) is
+// emitted as edges (run head, head of a touching run of the four forward rows, or the voxel
+// across the chunk end); lanes drop links the previous lane already made, each warp reserves
+// its edges with one shared-memory atomic and each block with one global atomic.
 struct EdgeBuf {
   int2* e;
   unsigned cap;
@@ -87,44 +84,36 @@ __global__ void __launch_bounds__(TX* TY)
   const int tx = lane, ty = t >> 5;
   const int gx = X0 + tx, gy = Y0 + ty;
   const bool inxy = gx < nx && gy < ny;
-  const bool edge_xy = gx == 0 || gx == nx - 1 || gy == 0 || gy == ny - 1;
   const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
-  float w[27];  // w[k]: neighbour k = (dz+1)*9 + (dy+1)*3 + (dx+1) of the current voxel
-#pragma unroll
-  for (int k = 0; k < 18; ++k) w[k] = s[k / 9][ty + (k / 3) % 3][tx + k % 3];
-#pragma unroll
   for (int tz = 0; tz < TZ; ++tz) {
-#pragma unroll
-    for (int k = 18; k < 27; ++k) w[k] = s[tz + 2][ty + (k / 3) % 3][tx + k % 3];
     const int gz = Z0 + tz;
     const bool valid = inxy && gz < nz;
     const int ci = gz * nxy + gy * nx + gx;
-    const float cv = w[kSelf];
     if (valid) {
+      const float* c0 = &s[tz + 1][ty + 1][tx + 1];
+      const float cv = *c0;
       const int cls = cv > 0.0f ? CLS_PORE
                                 : (cv < thr ? CLS_MARKER : (!(cv >= 0.0f) ? CLS_FLOOD : CLS_ZERO));
-      const bool need = ALL_ASCENT || !(cv <= 0.0f);
-      // maximum / minimum of the 26 neighbours as balanced trees (NaNs drop out of fmaxf/fminf)
-      float a[13], b[13];
-#pragma unroll
-      for (int i = 0; i < 13; ++i) {
-        const float p = w[i], q = w[26 - i];
-        a[i] = fmaxf(p, q);
-        b[i] = fminf(p, q);
-      }
-#pragma unroll
-      for (int h = 1; h < 13; h <<= 1)
-#pragma unroll
-        for (int i = 0; i + h < 13; i += 2 * h) {
-          a[i] = fmaxf(a[i], a[i + h]);
-          b[i] = fminf(b[i], b[i + h]);
-        }
-      const float vmax = fmaxf(a[0], cv);
       int bk = kSelf;
-      if (need) {
-        if (!(cv == cv) || edge_xy || gz == 0 || gz == nz - 1) {
-          // NaN centre or wrapped neighbours: the reference's comparison sequence
-          float bv = cv;
+      // ascent: every voxel for the flow basins, otherwise where a walk starts (sdf > 0) or a
+      // peak can sit (!(sdf <= 0), NaN included)
+      if (ALL_ASCENT || !(cv <= 0.0f)) {
+        float bv = cv;
+        bool tie = false;
+        // strict scan; any equality with the running maximum takes the exact tie-aware scan
+#pragma unroll
+        for (int k = 0; k < 27; ++k) {
+          if (k == kSelf) continue;
+          const float nv = c0[(k / 9 - 1) * (HY * HX) + ((k / 3) % 3 - 1) * HX + (k % 3 - 1)];
+          tie |= (nv == bv);
+          if (nv > bv) {
+            bv = nv;
+            bk = k;
+          }
+        }
+        if (tie) {
+          bv = cv;
+          bk = kSelf;
           int bi = ci;
 #pragma unroll 1
           for (int k = 0; k < 27; ++k) {
@@ -141,100 +130,99 @@ __global__ void __launch_bounds__(TX* TY)
               bi = ni;
             }
           }
-        } else {
-#pragma unroll
-          for (int k = 0; k < 27; ++k) bk = (w[k] == vmax) ? k : bk;
         }
         nxt[ci] = bk == kSelf ? ci
                               : wz[tz + bk / 9] * nxy + wy[ty + (bk / 3) % 3] * nx + wx[tx + bk % 3];
         if (!(cv <= 0.0f) && bk == kSelf) atomicOr(&peakbits[ci >> 5], 1u << (ci & 31));
       }
-      // a shallow-solid voxel with a marker neighbour is a flood seed (NaN is never < thr)
-      const bool seed = cls == CLS_FLOOD && b[0] < thr;
+      bool seed = false;  // a shallow-solid voxel with a marker neighbour (NaN is never < thr)
+      if (cls == CLS_FLOOD) {
+        float vmin = c0[-(HY * HX) - HX - 1];
+#pragma unroll
+        for (int k = 1; k < 27; ++k) {
+          if (k == kSelf) continue;
+          vmin = fminf(vmin, c0[(k / 9 - 1) * (HY * HX) + ((k / 3) % 3 - 1) * HX + (k % 3 - 1)]);
+        }
+        seed = vmin < thr;
+      }
       code[ci] = make_code(bk, cls, seed);
     }
     // marker runs of this chunk row
     const unsigned m = rowm[tz + 1][ty + 1];
     const bool marker = valid && ((m >> lane) & 1u);
     const int hl = marker ? 31 - __clz((m & ~(m << 1)) & upto) : 0;
-    const int rowbase = gz * nxy + gy * nx;
-    if (valid) L[ci] = marker ? rowbase + X0 + hl : kBig;
-    if (__any_sync(0xffffffffu, marker)) {
-      // run heads list the runs their dilated extent touches in the four forward rows
-      const bool is_head = marker && hl == lane;
-      int rep[10];
-      int nrep = 0;
-      if (is_head) {
-        const unsigned valid_m = (TX - 1 < nx - 1 - X0) ? 0xffffffffu
-                                                        : ((2u << (nx - 1 - X0)) - 1u);
-        const unsigned mv = m & valid_m;
-        const int e = lane + __ffsll(~((unsigned long long)mv >> lane)) - 2;  // run's last lane
-        const int head_g = rowbase + X0 + lane;
-        // a full list spills straight to the global edge buffer (adversarial run patterns)
-        auto add = [&](int r) {
-          if (nrep < 10) {
-            rep[nrep++] = r;
-          } else {
-            const unsigned g = atomicAdd(&cnt[CNT_EDGES], 1u);
-            if (g < eb.cap) eb.e[g] = make_int2(head_g, r);
-          }
-        };
-        // +x neighbour across the chunk end (or the periodic wrap inside this chunk)
-        if ((e == 31 || X0 + e == nx - 1) && s[tz + 1][ty + 1][e + 2] < thr)
-          add(rowbase + wx[e + 2]);
+    const int head = gz * nxy + gy * nx + X0 + hl;
+    if (valid) L[ci] = marker ? head : kBig;
+    if (!__any_sync(0xffffffffu, marker)) continue;
+    // links: up to two touching runs per forward row plus the +x voxel across the chunk end
+    int rep[9];
+    unsigned have = 0;
 #pragma unroll
-        for (int f = 0; f < 4; ++f) {  // forward rows (dy,dz) = (1,0), (-1,1), (0,1), (1,1)
-          const int sy = ty + 1 + ((f == 0 || f == 3) ? 1 : (f == 1 ? -1 : 0));
-          const int sz = tz + 1 + (f == 0 ? 0 : 1);
-          const unsigned m2 = rowm[sz][sy];
-          const unsigned hb = rowh[sz][sy];
-          const int rowg = wz[sz] * nxy + wy[sy] * nx;
-          const int lo = lane - 1, hi = e + 1;  // dilated extent in chunk positions
-          if (lo < 0) {
-            if (hb & 1u) add(rowg + wx[0]);
-          } else if ((m2 >> lo) & 1u) {
-            const unsigned st2 = m2 & ~(m2 << 1);
-            const int p = 31 - __clz(st2 & (lo == 31 ? 0xffffffffu : ((2u << lo) - 1u)));
-            add(rowg + wx[p + 1]);
-          }
-          // runs of the forward row starting inside (lo, min(hi, 31)]
-          const int top = hi > 31 ? 31 : hi;
-          unsigned starts = (m2 & ~(m2 << 1)) & (top == 31 ? 0xffffffffu : ((2u << top) - 1u)) &
-                            ~((2u << lo) - 1u);
-          if (lo < 0) starts = (m2 & ~(m2 << 1)) & (top == 31 ? 0xffffffffu : ((2u << top) - 1u));
-          while (starts) {
-            const int p = __ffs(starts) - 1;
-            starts &= starts - 1;
-            add(rowg + wx[p + 1]);
-          }
-          if (hi > 31 && (hb & 2u) && !((m2 >> 31) & 1u)) add(rowg + wx[HX - 1]);
-        }
-      }
-      // warp-compacted staging: one shared-memory reservation per warp
-      unsigned incl = (unsigned)nrep;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-      }
-      const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
-      unsigned base = 0;
-      if (lane == 0 && total) base = atomicAdd(&nstage, total);
-      base = __shfl_sync(0xffffffffu, base, 0) + incl - (unsigned)nrep;
-      const int head = rowbase + X0 + hl;
-      for (int j = 0; j < nrep; ++j) {
-        const int2 ed = make_int2(head, rep[j]);
-        if (base < (unsigned)kStage) {
-          stage[base] = ed;
+    for (int f = 0; f < 4; ++f) {  // forward rows (dy,dz) = (1,0), (-1,1), (0,1), (1,1)
+      const int sy = ty + 1 + ((f == 0 || f == 3) ? 1 : (f == 1 ? -1 : 0));
+      const int sz = tz + 1 + (f == 0 ? 0 : 1);
+      const unsigned m2 = rowm[sz][sy];
+      const unsigned hb = rowh[sz][sy];
+      const unsigned st2 = m2 & ~(m2 << 1);
+      int c0 = -2, c1 = -2;  // chunk positions; -1 / 32: the halo columns
+      if (marker) {
+        if ((m2 >> lane) & 1u) {
+          c0 = 31 - __clz(st2 & upto);
         } else {
-          const unsigned g = atomicAdd(&cnt[CNT_EDGES], 1u);
-          if (g < eb.cap) eb.e[g] = ed;
+          if (lane > 0) {
+            if ((m2 >> (lane - 1)) & 1u) c0 = 31 - __clz(st2 & (upto >> 1));
+          } else if (hb & 1u) {
+            c0 = -1;
+          }
+          if (lane < 31) {
+            if ((m2 >> (lane + 1)) & 1u) c1 = lane + 1;
+          } else if (hb & 2u) {
+            c1 = 32;
+          }
         }
-        ++base;
+      }
+      const int p0 = __shfl_up_sync(0xffffffffu, c0, 1);
+      const int p1 = __shfl_up_sync(0xffffffffu, c1, 1);
+      const int ph = __shfl_up_sync(0xffffffffu, head, 1);
+      const bool same = lane > 0 && ph == head;
+      const int rowg = wz[sz] * nxy + wy[sy] * nx;
+      if (c0 != -2 && !(same && (c0 == p0 || c0 == p1))) {
+        rep[2 * f] = rowg + wx[c0 + 1];
+        have |= 1u << (2 * f);
+      }
+      if (c1 != -2 && !(same && (c1 == p0 || c1 == p1))) {
+        rep[2 * f + 1] = rowg + wx[c1 + 1];
+        have |= 1u << (2 * f + 1);
       }
     }
+    if (marker && (lane == 31 || gx + 1 == nx) && s[tz + 1][ty + 1][tx + 2] < thr) {
+      rep[8] = gz * nxy + gy * nx + wx[tx + 2];
+      have |= 1u << 8;
+    }
+    // warp-compacted staging: one shared-memory reservation per warp
+    const unsigned mine = __popc(have);
+    unsigned incl = mine;
 #pragma unroll
-    for (int k = 0; k < 18; ++k) w[k] = w[k + 9];
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+    unsigned base = 0;
+    if (lane == 0 && total) base = atomicAdd(&nstage, total);
+    base = __shfl_sync(0xffffffffu, base, 0) + incl - mine;
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+      if (!((have >> j) & 1u)) continue;
+      const int2 e = make_int2(head, rep[j]);
+      if (base < (unsigned)kStage) {
+        stage[base] = e;
+      } else {
+        const unsigned g = atomicAdd(&cnt[CNT_EDGES], 1u);
+        if (g < eb.cap) eb.e[g] = e;
+      }
+      ++base;
+    }
   }
   __syncthreads();
   const unsigned ns = min(nstage, (unsigned)kStage);
@@ -283,28 +271,6 @@ __global__ void __launch_bounds__(256) k_ccl_all(Dims d, int* L, unsigned* err) 
       const unsigned peers = __match_any_sync(0xffffffffu, pk);
       if (pk != ~0ull && (__ffs(peers) - 1) == (int)lane_id()) uf_unite(L, a, b, err);
     }
-  }
-}
-
-// ---- pointer doubling of the ascent pointers: out = in o in, for the voxels whose pointer the
-// pipeline reads (every voxel when all_ascent, else those with !(sdf <= 0), i.e. pore-or-NaN
-// class bits with a computed direction). Two passes turn nxt into nxt4.
-template <bool ALL>
-__global__ void __launch_bounds__(256)
-    k_nxt_double(Dims d, const uint8_t* __restrict__ code, const int* __restrict__ in,
-                 int* __restrict__ out) {
-  const long long n = d.n();
-  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n;
-       v += (long long)gridDim.x * blockDim.x) {
-    if (!ALL) {
-      const int cls = code_cls(code[v]);
-      if (cls != CLS_PORE && cls != CLS_FLOOD) continue;  // FLOOD covers NaN (sdf unordered)
-      if (cls == CLS_FLOOD && code_dir(code[v]) == kSelf) {
-        out[v] = (int)v;  // NaN or a shallow-solid voxel without a computed pointer
-        continue;
-      }
-    }
-    out[v] = __ldg(&in[__ldg(&in[v])]);
   }
 }
 
@@ -854,19 +820,6 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
     PNM_CUDA(cudaGetLastError());
   }
   st->n_edges = n_edges;
-  {  // nxt -> nxt4 (the second buffer is the flood's tmp list, unused until the flood)
-    int* nxt2 = nullptr;
-    PNM_TRY(c.buf(S_TMP, n, &nxt2));
-    const unsigned g = grid_for(n, 256, c.sm_count);
-    if (all_ascent) {
-      k_nxt_double<true><<<g, 256, 0, s>>>(d, st->code, st->nxt, nxt2);
-      k_nxt_double<true><<<g, 256, 0, s>>>(d, st->code, nxt2, st->nxt);
-    } else {
-      k_nxt_double<false><<<g, 256, 0, s>>>(d, st->code, st->nxt, nxt2);
-      k_nxt_double<false><<<g, 256, 0, s>>>(d, st->code, nxt2, st->nxt);
-    }
-    c.launches += 2;
-  }
   k_resolve<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, st->code, st->nxt, L, key, keylist,
                                                           c.d_cnt); ++c.launches;
   PNM_CUDA(cudaGetLastError());
