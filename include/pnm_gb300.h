@@ -163,6 +163,61 @@ int pnm_extract_pores_noalloc(const float* d_sdf, int32_t nx, int32_t ny, int32_
                               pnm_pore* d_pores, int64_t pore_cap, int64_t* n_pores,
                               void* stream);
 
+/* ---- batched extraction ------------------------------------------------------------------
+ * No counterpart in the reference: its bindings (src/pnm_bindings.cpp:143-160) take one volume
+ * per call, so a caller with many volumes loops over extract_pore_network_k
+ * (src/pore_extraction.hpp:1011-1025). A batch is planned once for a fixed list of periodic
+ * volumes of any shapes; every device buffer is allocated at creation. Each run extracts all
+ * volumes with one launch per stage over a ragged volume table (per-volume wrap, per-volume
+ * label numbering), with the flood fixpoint in one persistent kernel and no host round trip
+ * inside the run; after the first run the whole run is replayed from a CUDA graph. The labels,
+ * pores and pairs of every volume are bit-identical to pnm_extract_pore_network on that volume
+ * alone. A batch owns its stream; calls on one batch must not overlap. */
+typedef struct pnm_batch pnm_batch;
+
+typedef struct {
+  int64_t voxel_offset;   /* first voxel of the volume in the batch SDF / label buffers */
+  int32_t nx, ny, nz;
+  int32_t n_pore_labels, n_solid_labels;
+  int32_t reserved;
+  int64_t pore_offset;    /* first pore record of the volume in the batch pore buffer */
+  int64_t n_pores;        /* pores of the volume (at most 1e6, the reference's max_pores) */
+  int64_t pair_offset;    /* first (label_a, label_b) pair of the volume in the pair buffer */
+  int64_t n_pairs;
+} pnm_batch_volume;
+
+#define PNM_BATCH_NO_GRAPH 1 /* enqueue the stages on every run instead of replaying a graph */
+
+/* Device bytes a batch of these shapes allocates at creation (before any capacity growth). */
+int pnm_batch_plan_bytes(int32_t n_volumes, const int32_t* dims_xyz, int64_t* bytes);
+/* dims_xyz: 3 per volume (nx, ny, nz); origin_xyz / spacing_xyz: 3 per volume. */
+int pnm_batch_create(pnm_ctx* ctx, int32_t n_volumes, const int32_t* dims_xyz,
+                     const float* origin_xyz, const float* spacing_xyz, int32_t flags,
+                     pnm_batch** out);
+void pnm_batch_destroy(pnm_batch* b);
+const char* pnm_batch_last_error(const pnm_batch* b);
+/* The batch's CUDA stream (cudaStream_t); every batch call is ordered on it. */
+void* pnm_batch_stream(const pnm_batch* b);
+/* Copies volume i's SDF (float32, x fastest) from host memory into the batch (async). */
+int pnm_batch_set_sdf(pnm_batch* b, int32_t i, const float* sdf);
+/* The batch SDF buffer on the device (volume i at voxel_offset) and its length in floats. */
+int pnm_batch_sdf_dev(pnm_batch* b, float** d_sdf, int64_t* n);
+/* Enqueues one run (async); pnm_batch_wait completes it (and re-runs once if a capacity grew). */
+int pnm_batch_launch(pnm_batch* b);
+int pnm_batch_wait(pnm_batch* b);
+int pnm_batch_run(pnm_batch* b); /* launch + wait */
+/* Results of the last completed run. */
+int pnm_batch_volume_info(const pnm_batch* b, int32_t i, pnm_batch_volume* out);
+/* Device buffers of the last run: pore records, labels (voxel_offset-based), pairs (2 ints each). */
+int pnm_batch_results_dev(const pnm_batch* b, pnm_pore** d_pores, int32_t** d_seg,
+                          int32_t** d_pairs);
+/* Copies volume i's results to host buffers sized from pnm_batch_volume_info (any may be null). */
+int pnm_batch_copy_out(pnm_batch* b, int32_t i, pnm_pore* pores, int32_t* seg, int32_t* pairs);
+/* launches: kernels of one run; calls: runs so far; voxels: batch voxels; workspace_bytes. */
+int pnm_batch_get_stats(const pnm_batch* b, pnm_stats* out);
+/* 1 if runs replay a CUDA graph, 0 if they enqueue the stages (flag, or capture unavailable). */
+int pnm_batch_uses_graph(const pnm_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -90,12 +90,46 @@ pnm_flow_result_free = _sig("pnm_flow_result_free", None, _P(PnmFlowResult))
 pnm_extract_pores_noalloc = _sig("pnm_extract_pores_noalloc", ctypes.c_int, _vp, _i32, _i32, _i32,
                                  _vp, _vp, _vp, _i64, _P(_i64), _vp)
 
+
+
+class PnmBatchVolume(ctypes.Structure):
+    _fields_ = [("voxel_offset", _i64), ("nx", _i32), ("ny", _i32), ("nz", _i32),
+                ("n_pore_labels", _i32), ("n_solid_labels", _i32), ("reserved", _i32),
+                ("pore_offset", _i64), ("n_pores", _i64), ("pair_offset", _i64),
+                ("n_pairs", _i64)]
+
+
+PNM_BATCH_NO_GRAPH = 1
+pnm_batch_plan_bytes = _sig("pnm_batch_plan_bytes", ctypes.c_int, _i32, _vp, _P(_i64))
+pnm_batch_create = _sig("pnm_batch_create", ctypes.c_int, _vp, _i32, _vp, _vp, _vp, _i32,
+                        _P(_vp))
+pnm_batch_destroy = _sig("pnm_batch_destroy", None, _vp)
+pnm_batch_last_error = _sig("pnm_batch_last_error", ctypes.c_char_p, _vp)
+pnm_batch_stream = _sig("pnm_batch_stream", _vp, _vp)
+pnm_batch_set_sdf = _sig("pnm_batch_set_sdf", ctypes.c_int, _vp, _i32, _vp)
+pnm_batch_sdf_dev = _sig("pnm_batch_sdf_dev", ctypes.c_int, _vp, _P(_vp), _P(_i64))
+pnm_batch_launch = _sig("pnm_batch_launch", ctypes.c_int, _vp)
+pnm_batch_wait = _sig("pnm_batch_wait", ctypes.c_int, _vp)
+pnm_batch_run = _sig("pnm_batch_run", ctypes.c_int, _vp)
+pnm_batch_volume_info = _sig("pnm_batch_volume_info", ctypes.c_int, _vp, _i32,
+                             _P(PnmBatchVolume))
+pnm_batch_results_dev = _sig("pnm_batch_results_dev", ctypes.c_int, _vp, _P(_vp), _P(_vp),
+                             _P(_vp))
+pnm_batch_copy_out = _sig("pnm_batch_copy_out", ctypes.c_int, _vp, _i32, _vp, _vp, _vp)
+pnm_batch_get_stats = _sig("pnm_batch_get_stats", ctypes.c_int, _vp, _P(PnmStats))
+pnm_batch_uses_graph = _sig("pnm_batch_uses_graph", ctypes.c_int, _vp)
+
 #: every symbol include/pnm_gb300.h declares
 EXPORTED = ["pnm_ctx_create", "pnm_ctx_destroy", "pnm_last_error", "pnm_ctx_set_stream",
             "pnm_ctx_trim", "pnm_execution_space", "pnm_free", "pnm_extract_pores",
             "pnm_segment_volume", "pnm_extract_topology", "pnm_extract_pore_network",
             "pnm_extract_network_flow", "pnm_flow_result_free", "pnm_extract_pore_network_dev",
-            "pnm_segment_volume_dev", "pnm_ctx_get_stats", "pnm_extract_pores_noalloc"]
+            "pnm_segment_volume_dev", "pnm_ctx_get_stats", "pnm_extract_pores_noalloc",
+            "pnm_batch_plan_bytes", "pnm_batch_create", "pnm_batch_destroy",
+            "pnm_batch_last_error", "pnm_batch_stream", "pnm_batch_set_sdf", "pnm_batch_sdf_dev",
+            "pnm_batch_launch", "pnm_batch_wait", "pnm_batch_run", "pnm_batch_volume_info",
+            "pnm_batch_results_dev", "pnm_batch_copy_out", "pnm_batch_get_stats",
+            "pnm_batch_uses_graph"]
 
 
 class PnmError(RuntimeError):

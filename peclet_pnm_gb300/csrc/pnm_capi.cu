@@ -13,10 +13,6 @@
 
 #include "pnm_ctx.h"
 
-struct pnm_ctx {
-  pnm::Ctx c;
-};
-
 namespace pnm {
 
 Status cuda_status(cudaError_t e, const char* what) {

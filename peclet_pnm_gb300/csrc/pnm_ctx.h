@@ -39,6 +39,7 @@ enum ErrFlag : unsigned {
   ERRF_HASH_FULL = 2u,      // the pair hash set ran out of probes
   ERRF_FLOOD_LIMIT = 4u,    // the flood wavefront exceeded its sweep limit
   ERRF_FACE_LIMIT = 8u,     // a face-CCL find/unite exceeded its iteration limit
+  ERRF_BARRIER = 16u,       // a grid barrier of a persistent kernel timed out
 };
 
 // ---- counter block (device ints; one copy per context) ------------------------------------------
@@ -51,6 +52,9 @@ enum Counter : int {
   CNT_EDGES,         // marker-CCL edges emitted by the SDF pass
   CNT_FLOW_SPARE0,
   CNT_FLOW_SPARE1,
+  CNT_SWEEPS,        // flood sweeps run by the persistent flood loop
+  CNT_BAR0,          // grid barrier of the persistent flood loop: arrivals
+  CNT_BAR1,          //   and generation
   CNT_COUNT = 32
 };
 
@@ -168,3 +172,8 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
                         const FlowInputs& in, FlowOutputsHost* out);
 
 }  // namespace pnm
+
+// The opaque handle of the C ABI.
+struct pnm_ctx {
+  pnm::Ctx c;
+};

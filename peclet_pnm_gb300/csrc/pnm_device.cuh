@@ -121,6 +121,54 @@ __device__ __forceinline__ int chase_root(const int* __restrict__ nxt, int v) {
   return cur;
 }
 
+// ---- grid barrier for persistent (cooperatively launched) kernels ---------------------------------
+// bar[0] counts arrivals, bar[1] is the generation. Every wait is bounded: after kBarrierNs of
+// global time the waiting block sets ERRF_BARRIER and returns false, so a kernel whose blocks were
+// not all resident ends with an error status instead of spinning.
+constexpr unsigned long long kBarrierNs = 1000000000ull;  // 1 s
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* err) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    const unsigned gen = ld_acquire_u32(&bar[1]);  // cannot advance before this block arrives
+    __threadfence();
+    if (atomicAdd(&bar[0], 1u) == gridDim.x - 1) {
+      atomicExch(&bar[0], 0u);
+      __threadfence();
+      atomicAdd(&bar[1], 1u);
+    } else {
+      const unsigned long long t0 = global_ns();
+      while (ld_acquire_u32(&bar[1]) == gen) {
+        if (global_ns() - t0 > kBarrierNs) {
+          atomicOr(err, ERRF_BARRIER);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
 // ---- warp helpers -------------------------------------------------------------------------------
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31; }
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -277,9 +325,13 @@ constexpr int RS_THREADS = 256;
 constexpr int RS_ROUNDS = 16;
 constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
 
+// m_dev (optional): the live key count on the device, at most m; tiles past it stay empty, so a
+// sort sized for a capacity can be enqueued before the count is known (graph capture).
 static __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint64_t* keys, long long m,
-                                                        int shift, unsigned* hist) {
+                                                        int shift, unsigned* hist,
+                                                        const unsigned* m_dev) {
   __shared__ unsigned h[256];
+  if (m_dev) m = min(m, (long long)*m_dev);
   h[threadIdx.x] = 0;
   __syncthreads();
   const long long base = (long long)blockIdx.x * RS_TILE;
@@ -294,8 +346,10 @@ static __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint64_t* k
 static __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t* kin, const unsigned* vin,
                                                            uint64_t* kout, unsigned* vout,
                                                            long long m, int shift,
-                                                           const unsigned* offs) {
+                                                           const unsigned* offs,
+                                                           const unsigned* m_dev) {
   __shared__ unsigned base[256];
+  if (m_dev) m = min(m, (long long)*m_dev);
   __shared__ unsigned wc[RS_THREADS / 32][257];
   const int wid = threadIdx.x >> 5;
   base[threadIdx.x] = offs[(long long)threadIdx.x * gridDim.x + blockIdx.x];
@@ -341,8 +395,9 @@ static __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t
 // scan_tmp ceil(256*nb/SCAN_TILE)+1.
 inline bool radix_sort(uint64_t* ka, unsigned* va, uint64_t* kb, unsigned* vb, long long m,
                        int lo_bit, int hi_bit, unsigned* hist, unsigned* scan_tmp,
-                       cudaStream_t s, long long* launches) {
-  if (m <= 1) return false;
+                       cudaStream_t s, long long* launches, const unsigned* m_dev = nullptr) {
+  if (m <= 1 && !m_dev) return false;
+  if (m <= 0) return false;
   const long long nb = (m + RS_TILE - 1) / RS_TILE;
   bool in_b = false;
   for (int sh = lo_bit; sh < hi_bit; sh += 8) {
@@ -350,9 +405,9 @@ inline bool radix_sort(uint64_t* ka, unsigned* va, uint64_t* kb, unsigned* vb, l
     unsigned* vi = in_b ? vb : va;
     uint64_t* ko = in_b ? ka : kb;
     unsigned* vo = in_b ? va : vb;
-    k_rs_hist<<<(unsigned)nb, RS_THREADS, 0, s>>>(ki, m, sh, hist);
+    k_rs_hist<<<(unsigned)nb, RS_THREADS, 0, s>>>(ki, m, sh, hist, m_dev);
     exclusive_scan(ValueOf{hist}, 256 * nb, hist, scan_tmp, s, launches);
-    k_rs_scatter<<<(unsigned)nb, RS_THREADS, 0, s>>>(ki, vi, ko, vo, m, sh, hist);
+    k_rs_scatter<<<(unsigned)nb, RS_THREADS, 0, s>>>(ki, vi, ko, vo, m, sh, hist, m_dev);
     *launches += 2;
     in_b = !in_b;
   }

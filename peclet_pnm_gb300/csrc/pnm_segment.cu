@@ -15,6 +15,7 @@
 
 #include "pnm_ctx.h"
 #include "pnm_device.cuh"
+#include "pnm_geo.cuh"
 
 namespace pnm {
 
@@ -41,9 +42,9 @@ struct EdgeBuf {
 };
 constexpr int kStage = 2048;  // edges staged per block; a full stage spills straight to global
 
-template <bool ALL_ASCENT>
+template <bool ALL_ASCENT, class G>
 __global__ void __launch_bounds__(TX* TY)
-    k_sdf_pass(const float* __restrict__ sdf, Dims d, float thr, uint8_t* __restrict__ code,
+    k_sdf_pass(const float* __restrict__ sdf, G geo, uint8_t* __restrict__ code,
                int* __restrict__ nxt, int* __restrict__ L, uint32_t* __restrict__ peakbits,
                EdgeBuf eb, unsigned* cnt) {
   constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2, NT = TX * TY;
@@ -53,12 +54,24 @@ __global__ void __launch_bounds__(TX* TY)
   __shared__ unsigned char rowh[HZ][HY];  // bit 0: marker at x = X0-1; bit 1: at x = X0+32
   __shared__ int2 stage[kStage];
   __shared__ unsigned nstage, gbase;
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const Box bx = geo.tile(blockIdx.x, TX, TY, TZ, false);
+  const int off = bx.off;  // the volume's first global voxel id: added to every stored id
+  const float thr = bx.thr;
+  sdf += off;
+  code += off;
+  nxt += off;
+  L += off;
+  peakbits += off >> 5;
+  const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
   const int nxy = nx * ny;
-  const int X0 = blockIdx.x * TX, Y0 = blockIdx.y * TY, Z0 = blockIdx.z * TZ;
+  const int X0 = bx.X0, Y0 = bx.Y0, Z0 = bx.Z0;
   const int t = threadIdx.x;
   const int lane = t & 31;  // == tx (TX == 32)
   if (t == 0) nstage = 0;
+  if (G::kBatch && bx.first) {  // the gap up to the next volume: never-labelled ZERO codes
+    const int n = nx * ny * nz;
+    for (int i = n + t; i < ((n + 31) & ~31); i += NT) code[i] = make_code(kSelf, CLS_ZERO, false);
+  }
   if (t < HX) wx[t] = ((X0 - 1 + t) % nx + nx) % nx;
   if (t < HY) wy[t] = ((Y0 - 1 + t) % ny + ny) % ny;
   if (t < HZ) wz[t] = ((Z0 - 1 + t) % nz + nz) % nz;
@@ -131,8 +144,9 @@ __global__ void __launch_bounds__(TX* TY)
             }
           }
         }
-        nxt[ci] = bk == kSelf ? ci
-                              : wz[tz + bk / 9] * nxy + wy[ty + (bk / 3) % 3] * nx + wx[tx + bk % 3];
+        nxt[ci] = off + (bk == kSelf ? ci
+                                     : wz[tz + bk / 9] * nxy + wy[ty + (bk / 3) % 3] * nx +
+                                           wx[tx + bk % 3]);
         if (!(cv <= 0.0f) && bk == kSelf) atomicOr(&peakbits[ci >> 5], 1u << (ci & 31));
       }
       bool seed = false;  // a shallow-solid voxel with a marker neighbour (NaN is never < thr)
@@ -151,7 +165,7 @@ __global__ void __launch_bounds__(TX* TY)
     const unsigned m = rowm[tz + 1][ty + 1];
     const bool marker = valid && ((m >> lane) & 1u);
     const int hl = marker ? 31 - __clz((m & ~(m << 1)) & upto) : 0;
-    const int head = gz * nxy + gy * nx + X0 + hl;
+    const int head = off + gz * nxy + gy * nx + X0 + hl;
     if (valid) L[ci] = marker ? head : kBig;
     if (!__any_sync(0xffffffffu, marker)) continue;
     // links: up to two touching runs per forward row plus the +x voxel across the chunk end
@@ -214,7 +228,7 @@ __global__ void __launch_bounds__(TX* TY)
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
       if (!((have >> j) & 1u)) continue;
-      const int2 e = make_int2(head, rep[j]);
+      const int2 e = make_int2(head, off + rep[j]);
       if (base < (unsigned)kStage) {
         stage[base] = e;
       } else {
@@ -247,16 +261,22 @@ __global__ void __launch_bounds__(256) k_ccl_edges(const int2* __restrict__ e, c
 
 // Fallback when the edge buffer overflowed (adversarial marker patterns): every marker unites
 // with its 13 forward periodic neighbours directly; lanes proposing the same (parent, parent)
-// link issue one union.
-__global__ void __launch_bounds__(256) k_ccl_all(Dims d, int* L, unsigned* err) {
-  const long long n = d.n();
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
+// link issue one union. Launched unconditionally inside a captured batch: it returns at once
+// unless the edge count exceeded the buffer.
+template <class G>
+__global__ void __launch_bounds__(256)
+    k_ccl_all(G geo, long long n, int* L, const unsigned* n_edges_p, unsigned cap, unsigned* err) {
+  if (n_edges_p && *n_edges_p <= cap) return;
   for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
        base += (long long)gridDim.x * blockDim.x) {
     const long long vl = base + threadIdx.x;
     const int v = (int)vl;
-    const int a = vl < n ? ld_relaxed(&L[v]) : kBig;
-    const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+    int off = 0, nx = 1, ny = 1, nz = 1;
+    if (vl < n) geo.locate(v, off, nx, ny, nz);
+    const int lv = v - off;
+    const bool inside = vl < n && lv < nx * ny * nz;  // not in the gap after a volume
+    const int a = inside ? ld_relaxed(&L[v]) : kBig;
+    const int x = lv % nx, y = (lv / nx) % ny, z = lv / (nx * ny);
 #pragma unroll 1
     for (int k = 0; k < 13; ++k) {
       const int dz = k < 9 ? 1 : 0;
@@ -265,7 +285,8 @@ __global__ void __launch_bounds__(256) k_ccl_all(Dims d, int* L, unsigned* err) 
       unsigned long long pk = ~0ull;
       int b = kBig;
       if (a != kBig) {
-        b = ld_relaxed(&L[(wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx)]);
+        b = ld_relaxed(&L[off + (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx +
+                          wrap1(x + dx, nx)]);
         if (b != kBig && b != a) pk = ((unsigned long long)(unsigned)a << 32) | (unsigned)b;
       }
       const unsigned peers = __match_any_sync(0xffffffffu, pk);
@@ -342,15 +363,20 @@ __global__ void __launch_bounds__(256)
 // (layer 2) and from each previous layer (t >= 3). Discovery marks a layer PENDING, assignment
 // computes its labels into `tmp`, and the next discovery publishes them, so no voxel ever sees a
 // same-sweep label — exactly the double-buffered Jacobi sweep.
+template <class G>
 __global__ void __launch_bounds__(TX* TY)
-    k_flood_seed(Dims d, const uint8_t* __restrict__ code, int* __restrict__ key, int* L,
+    k_flood_seed(G geo, const uint8_t* __restrict__ code, int* __restrict__ key, int* L,
                  int* __restrict__ ulist, unsigned* cnt) {
   constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2, NT = TX * TY;
   __shared__ int mk[HZ][HY][HX];  // marker neighbours' keys (~root), INT_MIN elsewhere
   __shared__ int wx[HX], wy[HY], wz[HZ];
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const Box bx = geo.tile(blockIdx.x, TX, TY, TZ, false);
+  const int off = bx.off;
+  code += off;
+  key += off;
+  const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
   const int nxy = nx * ny;
-  const int X0 = blockIdx.x * TX, Y0 = blockIdx.y * TY, Z0 = blockIdx.z * TZ;
+  const int X0 = bx.X0, Y0 = bx.Y0, Z0 = bx.Z0;
   const int t = threadIdx.x;
   const int lane = t & 31;
   if (t < HX) wx[t] = ((X0 - 1 + t) % nx + nx) % nx;
@@ -393,34 +419,38 @@ __global__ void __launch_bounds__(TX* TY)
           key[ci] = bestk;
           const int lab = ~bestk;
           // first appearance: the label's minimum starts at its root id L[lab] == lab
-          if (ci < lab) atomicMin(&L[lab], ci);
+          if (off + ci < lab) atomicMin(&L[lab], off + ci);
         } else {
           rest = true;
         }
       }
     }
     const int pos = warp_append(&cnt[CNT_FRONT_SPARE], rest);
-    if (rest) ulist[pos] = ci;
+    if (rest) ulist[pos] = off + ci;
   }
 }
 
 // layer 2: listed flood voxels with a seed neighbour (they have no marker neighbour)
+template <class G>
 __global__ void __launch_bounds__(256)
-    k_flood_layer2(Dims d, const uint8_t* __restrict__ code, int* key,
+    k_flood_layer2(G geo, const uint8_t* __restrict__ code, int* key,
                    const int* __restrict__ ulist, const unsigned* nu_p, int* __restrict__ fout,
                    unsigned* nout_p) {
   const unsigned nu = *nu_p;
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nu;
        i += (long long)gridDim.x * blockDim.x) {
     const int v = ulist[i];
-    const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+    int off, nx, ny, nz;
+    geo.locate(v, off, nx, ny, nz);
+    const int lv = v - off;
+    const int x = lv % nx, y = (lv / nx) % ny, z = lv / (nx * ny);
     bool hit = false;
     for (int dz = -1; dz <= 1 && !hit; ++dz)
       for (int dy = -1; dy <= 1 && !hit; ++dy)
         for (int dx = -1; dx <= 1; ++dx) {
           if (!dx && !dy && !dz) continue;
-          const int u = (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx);
+          const int u =
+              off + (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx);
           const uint8_t cu = __ldg(&code[u]);
           if (code_cls(cu) == CLS_FLOOD && code_seed(cu)) {
             hit = true;
@@ -434,55 +464,120 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Flood label of a layer voxel v: the smallest label (largest solid key) among its neighbours
+// labelled before this sweep. COH: loads bypass L1 (the persistent loop reads what other blocks
+// wrote earlier in the same launch).
+template <bool COH, class G>
+__device__ __forceinline__ int flood_assign_one(const G& geo, const int* key, int v) {
+  int off, nx, ny, nz;
+  geo.locate(v, off, nx, ny, nz);
+  const int lv = v - off;
+  const int x = lv % nx, y = (lv / nx) % ny, z = lv / (nx * ny);
+  int bestk = INT_MIN;
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        if (!dx && !dy && !dz) continue;
+        const int u = off + (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx);
+        const int k = COH ? ld_relaxed(&key[u]) : key[u];
+        if (key_is_solid(k)) bestk = max(bestk, k);
+      }
+  return ~bestk;
+}
+
+// Publishes v's label and discovers the next layer among its unlabelled flood neighbours.
+template <class G>
+__device__ __forceinline__ void flood_discover_one(const G& geo, const uint8_t* __restrict__ code,
+                                                   int* key, int* L, int v, int lab,
+                                                   int* __restrict__ fout, unsigned* nout_p) {
+  key[v] = ~lab;
+  if (v < lab) atomicMin(&L[lab], v);  // a label's minimum starts at its root id
+  int off, nx, ny, nz;
+  geo.locate(v, off, nx, ny, nz);
+  const int lv = v - off;
+  const int x = lv % nx, y = (lv / nx) % ny, z = lv / (nx * ny);
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        if (!dx && !dy && !dz) continue;
+        const int u = off + (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx);
+        if (code_cls(__ldg(&code[u])) != CLS_FLOOD) continue;
+        if (ld_relaxed(&key[u]) != KEY_NONE) continue;
+        if (atomicCAS(&key[u], KEY_NONE, KEY_PENDING) == KEY_NONE) {
+          const unsigned pos = atomicAdd(nout_p, 1u);
+          fout[pos] = u;
+        }
+      }
+}
+
 // publishes the labels of layer t (from tmp) and discovers layer t+1 among its neighbours
+template <class G>
 __global__ void __launch_bounds__(256)
-    k_flood_discover(Dims d, const uint8_t* __restrict__ code, int* key, int* L,
+    k_flood_discover(G geo, const uint8_t* __restrict__ code, int* key, int* L,
                      const int* __restrict__ fin, const unsigned* nin_p, const int* tmp,
                      int* __restrict__ fout, unsigned* nout_p) {
   const unsigned nin = *nin_p;
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nin;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int v = fin[i];
-    const int lab = tmp[i];
-    key[v] = ~lab;
-    if (v < lab) atomicMin(&L[lab], v);  // a label's minimum starts at its root id
-    const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
-    for (int dz = -1; dz <= 1; ++dz)
-      for (int dy = -1; dy <= 1; ++dy)
-        for (int dx = -1; dx <= 1; ++dx) {
-          if (!dx && !dy && !dz) continue;
-          const int u = (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx);
-          if (code_cls(__ldg(&code[u])) != CLS_FLOOD) continue;
-          if (ld_relaxed(&key[u]) != KEY_NONE) continue;
-          if (atomicCAS(&key[u], KEY_NONE, KEY_PENDING) == KEY_NONE) {
-            const unsigned pos = atomicAdd(nout_p, 1u);
-            fout[pos] = u;
-          }
-        }
-  }
+       i += (long long)gridDim.x * blockDim.x)
+    flood_discover_one(geo, code, key, L, fin[i], tmp[i], fout, nout_p);
 }
 
+template <class G>
 __global__ void __launch_bounds__(256)
-    k_flood_assign(Dims d, const int* __restrict__ key, const int* __restrict__ f,
+    k_flood_assign(G geo, const int* __restrict__ key, const int* __restrict__ f,
                    const unsigned* n_p, int* __restrict__ tmp) {
   const unsigned nf = *n_p;
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nf;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int v = f[i];
-    const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
-    int bestk = INT_MIN;  // largest solid key == smallest label
-    for (int dz = -1; dz <= 1; ++dz)
-      for (int dy = -1; dy <= 1; ++dy)
-        for (int dx = -1; dx <= 1; ++dx) {
-          if (!dx && !dy && !dz) continue;
-          const int u = (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx);
-          const int k = key[u];
-          if (key_is_solid(k)) bestk = max(bestk, k);
-        }
-    tmp[i] = ~bestk;
+       i += (long long)gridDim.x * blockDim.x)
+    tmp[i] = flood_assign_one<false>(geo, key, f[i]);
+}
+
+// All remaining sweeps in one cooperatively launched kernel: per sweep, assign (layer -> tmp),
+// grid barrier, publish + discover (next layer), grid barrier; it ends when a layer is empty, so
+// no host round trip sits between sweeps. The frontier starts in (fa, cnt[CNT_FRONT0]);
+// cnt[CNT_SWEEPS] receives 1 + the number of layer sweeps.
+template <class G>
+__global__ void __launch_bounds__(256)
+    k_flood_loop(G geo, const uint8_t* __restrict__ code, int* key, int* L, int* fa, int* fb,
+                 int* tmp, unsigned* cnt, int max_sweeps) {
+  unsigned* err = &cnt[CNT_ERR];
+  unsigned* bar = &cnt[CNT_BAR0];
+  int* fin = fa;
+  int* fout = fb;
+  int cin = CNT_FRONT0, cout = CNT_FRONT1;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  __shared__ unsigned s_nin;
+  __shared__ int s_stop;
+  int sweeps = 1;
+  while (true) {
+    if (threadIdx.x == 0) {  // one reading per block keeps every decision block-uniform
+      s_nin = ld_relaxed_u32(&cnt[cin]);
+      s_stop = s_nin == 0 || (ld_relaxed_u32(err) & ERRF_BARRIER) != 0;
+      if (!s_stop && sweeps >= max_sweeps) {
+        atomicOr(err, ERRF_FLOOD_LIMIT);
+        s_stop = 1;
+      }
+    }
+    __syncthreads();
+    const unsigned nin = s_nin;
+    if (s_stop) break;
+    for (long long i = tid; i < nin; i += stride)
+      tmp[i] = flood_assign_one<true>(geo, key, __ldcg(&fin[i]));
+    if (tid == 0) atomicExch(&cnt[cout], 0u);  // read by nobody since the last barrier
+    if (!grid_barrier(bar, err)) break;
+    for (long long i = tid; i < nin; i += stride)
+      flood_discover_one(geo, code, key, L, __ldcg(&fin[i]), __ldcg(&tmp[i]), fout, &cnt[cout]);
+    if (!grid_barrier(bar, err)) break;
+    int* t = fin;
+    fin = fout;
+    fout = t;
+    const int c = cin;
+    cin = cout;
+    cout = c;
+    ++sweeps;
   }
+  if (tid == 0) cnt[CNT_SWEEPS] = (unsigned)sweeps;
 }
 
 // ---- 5. first-appearance renumbering (pore_extraction.hpp:319-382) --------------------------------
@@ -501,7 +596,8 @@ __global__ void k_key_first(const int* __restrict__ keylist, const unsigned* nke
   }
 }
 
-__global__ void k_key_id(const int* __restrict__ keylist, const unsigned* nkeys_p, int* L,
+template <class G>
+__global__ void k_key_id(G geo, const int* __restrict__ keylist, const unsigned* nkeys_p, int* L,
                          const uint8_t* __restrict__ code, const uint32_t* firstP,
                          const unsigned* prefP, const uint32_t* firstS, const unsigned* prefS) {
   const unsigned nk = *nkeys_p;
@@ -509,8 +605,11 @@ __global__ void k_key_id(const int* __restrict__ keylist, const unsigned* nkeys_
        i += (long long)gridDim.x * blockDim.x) {
     const int k = keylist[i];
     const int m = L[k];
-    L[k] = code_cls(code[k]) == CLS_PORE ? (int)bitmap_rank(firstP, prefP, m) + 1
-                                         : -(int)bitmap_rank(firstS, prefS, m) - 1;
+    int off, nx, ny, nz;  // ranks count from the volume's first voxel (a word boundary)
+    geo.locate(k, off, nx, ny, nz);
+    L[k] = code_cls(code[k]) == CLS_PORE
+               ? (int)(bitmap_rank(firstP, prefP, m) - prefP[off >> 5]) + 1
+               : -(int)(bitmap_rank(firstS, prefS, m) - prefS[off >> 5]) - 1;
   }
 }
 
@@ -570,31 +669,40 @@ struct KeyLabels {
     const int src = 31 - __clz(leaders & (lane == 31 ? 0xffffffffu : ((2u << lane) - 1u)));
     return __shfl_sync(0xffffffffu, lab, src);
   }
+  // the same labels for a volume starting at global voxel `off` (keys are global ids)
+  __device__ KeyLabels at(int off) const { return KeyLabels{key + off, L}; }
 };
 struct SegLabels {
   const int* seg;
   __device__ int operator()(int v, bool active) const { return active ? __ldg(&seg[v]) : 0; }
+  __device__ SegLabels at(int off) const { return SegLabels{seg + off}; }
 };
 
 // One pass over 32 x 8 x 16 bricks (a warp owns a 32-voxel x-row and walks 16 z-planes): seg[v]
 // (optional) and every differing (+x,+y,+z) periodic face pair into the hash set. The +x label
 // comes from the neighbouring lane, the +z label is carried to the next plane. Lanes proposing
-// the pair of the previous lane skip their insert; lab_min/lab_max track the label range.
+// the pair of the previous lane skip their insert; lab_min/lab_max track the label range. In a
+// batch, pair labels are ordered as gbase(volume) + label, so one set holds every volume's pairs
+// and sorting it groups them by volume.
 __device__ __forceinline__ int lab_one(const KeyLabels& l, int v) {
   return label_of_key(l.L, __ldg(&l.key[v]));
 }
 __device__ __forceinline__ int lab_one(const SegLabels& l, int v) { return __ldg(&l.seg[v]); }
 
 constexpr int STX = 32, STY = 8, STZ = 16;
-template <class Lab>
+template <class G, class Lab>
 __global__ void __launch_bounds__(STX* STY)
-    k_seg_topo(Dims d, Lab lab, int* __restrict__ seg, int want_pairs, unsigned long long* table,
-               uint64_t mask, unsigned* cnt, int* range) {
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
+    k_seg_topo(G geo, Lab lab_all, int* __restrict__ seg, int want_pairs,
+               unsigned long long* table, uint64_t mask, unsigned* cnt, int* range) {
+  const Box bx = geo.tile(blockIdx.x, STX, STY, STZ, true);
+  const Lab lab = lab_all.at(bx.off);
+  if (seg) seg += bx.off;
+  const int gb = geo.gbase(bx.vol);
+  const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
   const int lane = threadIdx.x & 31;
-  const int x = blockIdx.x * STX + lane;
-  const int y = blockIdx.y * STY + (threadIdx.x >> 5);
-  const int z0 = blockIdx.z * STZ, z1 = min(z0 + STZ, nz);
+  const int x = bx.X0 + lane;
+  const int y = bx.Y0 + (threadIdx.x >> 5);
+  const int z0 = bx.Z0, z1 = min(z0 + STZ, nz);
   const bool in = x < nx && y < ny;
   const int xp = x + 1 >= nx ? 0 : x + 1;
   const int yp = y + 1 >= ny ? 0 : y + 1;
@@ -618,9 +726,10 @@ __global__ void __launch_bounds__(STX* STY)
         const int s1 = dd == 0 ? sx : (dd == 1 ? sy : sz);
         uint64_t pk = kEmpty;
         if (in && s1 != s0) {
-          pk = pair_key(s0, s1);
-          lmin = min(lmin, min(s0, s1));
-          lmax = max(lmax, max(s0, s1));
+          const int g0 = gb + s0, g1 = gb + s1;
+          pk = pair_key(g0, g1);
+          lmin = min(lmin, min(g0, g1));
+          lmax = max(lmax, max(g0, g1));
         }
         const uint64_t pp = __shfl_up_sync(0xffffffffu, pk, 1);
         if (pk != kEmpty && (lane == 0 || pp != pk))
@@ -740,6 +849,121 @@ void launch_pores_emit(const float* sdf, Dims d, const uint32_t* bits, const uns
                                     spacing[0], spacing[1], spacing[2], out, cap);
 }
 
+// ---- 8. batch bookkeeping -----------------------------------------------------------------------
+// One pore per set bit of the peak bitmap of a whole batch; a word's volume is found from its
+// first voxel (volumes start on word boundaries). Records land at the batch-wide rank, so each
+// volume's pores are contiguous and in voxel order.
+__global__ void k_pores_emit_batch(const float* __restrict__ sdf, VolTab geo,
+                                   const uint32_t* __restrict__ bits,
+                                   const unsigned* __restrict__ pref, long long words,
+                                   pnm_pore* __restrict__ out, long long cap) {
+  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < words;
+       w += (long long)gridDim.x * blockDim.x) {
+    uint32_t b = bits[w];
+    if (!b) continue;
+    unsigned r = pref[w];
+    const int vol = geo.vol_of((int)(w * 32));
+    const VolDesc& vd = geo.v[vol];
+    const int off = vd.off;
+    const Dims d{vd.nx, vd.ny, vd.nz};
+    while (b) {
+      const int j = __ffs(b) - 1;
+      b &= b - 1;
+      if ((long long)r < cap) {
+        const int v = (int)(w * 32 + j) - off;
+        const int ix = v % d.nx, iy = (v / d.nx) % d.ny, iz = v / (d.nx * d.ny);
+        out[r] = make_pore(sdf + off, d, ix, iy, iz, vd.ox, vd.oy, vd.oz, vd.sx, vd.sy, vd.sz,
+                           __ldg(&sdf[off + v]));
+      }
+      ++r;
+    }
+  }
+}
+
+__global__ void k_batch_init(int* range) {
+  range[0] = INT_MAX;
+  range[1] = INT_MIN;
+}
+
+// Per-volume label counts (rank differences over the volume's words) and pair-label bases: an
+// exclusive scan of nS + nP + 1 over the volumes, one block.
+__global__ void __launch_bounds__(SCAN_THREADS)
+    k_batch_labels(const VolDesc* __restrict__ v, VolResult* r, int nvol,
+                   const unsigned* __restrict__ prefP, const unsigned* __restrict__ prefS) {
+  __shared__ unsigned carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nvol; base += SCAN_THREADS) {
+    const int i = base + threadIdx.x;
+    unsigned np = 0, ns = 0;
+    if (i < nvol) {
+      const long long off = v[i].off, n = (long long)v[i].nx * v[i].ny * v[i].nz;
+      const long long w0 = off >> 5, w1 = (off + n + 31) >> 5;
+      np = prefP[w1] - prefP[w0];
+      ns = prefS[w1] - prefS[w0];
+    }
+    unsigned tot;
+    const unsigned ex = block_exclusive_sum(i < nvol ? np + ns + 1u : 0u, &tot);
+    if (i < nvol) {
+      r[i].n_pore_labels = np;
+      r[i].n_solid_labels = ns;
+      r[i].gstart = (int)(carry + ex);
+      r[i].gbase = (int)(carry + ex + ns);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) carry += tot;
+    __syncthreads();
+  }
+}
+
+// Sorted re-encoded pair keys -> (label_a, label_b) of their own volume.
+__global__ void k_pairs_decode_batch(const uint64_t* __restrict__ keys, const unsigned* m_p,
+                                     const int* range, int b, VolTab geo, int* __restrict__ out) {
+  const unsigned m = *m_p;
+  const int base = range[0];
+  const uint64_t lowmask = (1ull << b) - 1ull;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (long long)gridDim.x * blockDim.x) {
+    const uint64_t k = keys[i];
+    const int glo = (int)((uint32_t)(k >> b) + (uint32_t)base);
+    const int ghi = (int)((uint32_t)(k & lowmask) + (uint32_t)base);
+    const int gb = geo.r[geo.vol_of_label(glo)].gbase;
+    out[2 * i] = glo - gb;
+    out[2 * i + 1] = ghi - gb;
+  }
+}
+
+// Per-volume pore and pair ranges; thread 0 also records the batch's peak total.
+__global__ void k_batch_tail(const VolDesc* __restrict__ v, VolResult* r, int nvol,
+                             const unsigned* __restrict__ peakpref, long long words,
+                             const uint64_t* __restrict__ keys, const unsigned* m_p,
+                             const int* range, int b, unsigned* cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) cnt[CNT_FLOW_SPARE0] = peakpref[words];
+  if (i >= nvol) return;
+  const long long off = v[i].off, n = (long long)v[i].nx * v[i].ny * v[i].nz;
+  const long long w0 = off >> 5, w1 = (off + n + 31) >> 5;
+  r[i].peak0 = peakpref[w0];
+  r[i].n_peaks = peakpref[w1] - peakpref[w0];
+  const long long m = *m_p;
+  const long long base = range[0];
+  // first sorted pair whose smaller label is >= the label range start of volume j
+  auto lower = [&](int j) -> long long {
+    if (j >= nvol) return m;
+    const long long target = (long long)r[j].gstart - base;
+    long long lo = 0, hi = m;
+    while (lo < hi) {
+      const long long mid = (lo + hi) >> 1;
+      if ((long long)(keys[mid] >> b) < target) lo = mid + 1;
+      else hi = mid;
+    }
+    return lo;
+  };
+  const long long p0 = lower(i), p1 = lower(i + 1);
+  r[i].pair0 = (unsigned)p0;
+  r[i].n_pairs = (unsigned)(p1 - p0);
+}
+
 // =================================================================================================
 // host stages
 // =================================================================================================
@@ -751,13 +975,29 @@ inline unsigned grid_for(long long work, int threads, int sm_count, int per_sm =
   if (b < 1) b = 1;
   return (unsigned)b;
 }
-inline dim3 tile_grid(Dims d) {
-  return dim3((unsigned)((d.nx + TX - 1) / TX), (unsigned)((d.ny + TY - 1) / TY),
-              (unsigned)((d.nz + TZ - 1) / TZ));
+inline long long boxes_of(Dims d, int bx, int by, int bz) {
+  return (long long)((d.nx + bx - 1) / bx) * ((d.ny + by - 1) / by) * ((d.nz + bz - 1) / bz);
 }
 inline float marker_threshold(const float spacing[3]) {
   const float min_sp = std::min(spacing[0], std::min(spacing[1], spacing[2]));
   return -1.5f * min_sp;  // pore_extraction.hpp:163-164
+}
+
+// Cooperative launch of the persistent flood loop: as many blocks as can be resident at once.
+// blocks_per_sm stays well under the kernel's occupancy (8 blocks of 256 threads per SM), so that
+// loops of batches running on concurrent streams fit on the device together.
+template <class G>
+cudaError_t launch_flood_loop(G geo, const uint8_t* code, int* key, int* L, int* fa, int* fb,
+                              int* tmp, unsigned* cnt, int max_sweeps, int sm_count,
+                              long long work, cudaStream_t s, int blocks_per_sm = 2) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_flood_loop<G>, 256, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorCooperativeLaunchTooLarge;
+  const unsigned grid = grid_for(work, 256, sm_count, std::min(per_sm, blocks_per_sm));
+  void* args[] = {&geo, &code, &key, &L, &fa, &fb, &tmp, &cnt, &max_sweeps};
+  return cudaLaunchCooperativeKernel((const void*)k_flood_loop<G>, dim3(grid), dim3(256), args, 0,
+                                     s);
 }
 }  // namespace
 
@@ -779,14 +1019,15 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
   st->edges = eb.e;
   st->edge_cap = eb.cap;
   PNM_TRY(c.buf(S_NXT, n, &st->nxt));
+  const OneVol geo{d, marker_threshold(spacing)};
+  const unsigned tiles = (unsigned)boxes_of(d, TX, TY, TZ);
   if (all_ascent)
-    k_sdf_pass<true><<<tile_grid(d), TX * TY, 0, c.stream>>>(d_sdf, d, marker_threshold(spacing),
-                                                           st->code, st->nxt, L, st->peakbits,
-                                                           eb, c.d_cnt);
+    k_sdf_pass<true><<<tiles, TX * TY, 0, c.stream>>>(d_sdf, geo, st->code, st->nxt, L,
+                                                      st->peakbits, eb, c.d_cnt);
   else
-    k_sdf_pass<false><<<tile_grid(d), TX * TY, 0, c.stream>>>(d_sdf, d, marker_threshold(spacing),
-                                                            st->code, st->nxt, L, st->peakbits,
-                                                            eb, c.d_cnt); ++c.launches;
+    k_sdf_pass<false><<<tiles, TX * TY, 0, c.stream>>>(d_sdf, geo, st->code, st->nxt, L,
+                                                       st->peakbits, eb, c.d_cnt);
+  ++c.launches;
   PNM_CUDA(cudaGetLastError());
   st->idtab = L;
   return Status::ok();
@@ -799,6 +1040,7 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   cudaStream_t s = c.stream;
   PNM_CUDA(cudaMemsetAsync(c.d_cnt, 0, CNT_COUNT * sizeof(unsigned), s));
   PNM_TRY(run_sdf_pass(c, d_sdf, d, spacing, st, all_ascent));
+  const OneVol geo{d, marker_threshold(spacing)};
   int* L = st->idtab;
   int *key, *keylist, *f0, *f1, *tmp, *ulist;
   PNM_TRY(c.buf(S_ULIST, n, &ulist));
@@ -808,49 +1050,53 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   PNM_TRY(c.buf(S_FRONT1, n, &f1));
   PNM_TRY(c.buf(S_TMP, n, &tmp));
   st->key = key;
+  const unsigned vgrid = grid_for(n, 256, c.sm_count);
+  const unsigned tiles = (unsigned)boxes_of(d, TX, TY, TZ);
 
   k_ccl_edges<<<grid_for(n / 8 + 1, 256, c.sm_count), 256, 0, s>>>(
-      st->edges, &c.d_cnt[CNT_EDGES], st->edge_cap, L, &c.d_cnt[CNT_ERR]); ++c.launches;
-  PNM_CUDA(cudaGetLastError());
-  unsigned n_edges = 0;
-  PNM_CUDA(cudaMemcpyAsync(&n_edges, &c.d_cnt[CNT_EDGES], 4, cudaMemcpyDeviceToHost, s));
-  PNM_CUDA(cudaStreamSynchronize(s));
-  if (n_edges > st->edge_cap) {  // overflow: unite every forward adjacency directly
-    k_ccl_all<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, L, &c.d_cnt[CNT_ERR]); ++c.launches;
-    PNM_CUDA(cudaGetLastError());
-  }
-  st->n_edges = n_edges;
-  k_resolve<<<grid_for(n, 256, c.sm_count), 256, 0, s>>>(d, st->code, st->nxt, L, key, keylist,
-                                                          c.d_cnt); ++c.launches;
-  PNM_CUDA(cudaGetLastError());
-  k_flood_seed<<<tile_grid(d), TX * TY, 0, s>>>(d, st->code, key, L, ulist, c.d_cnt); ++c.launches;
+      st->edges, &c.d_cnt[CNT_EDGES], st->edge_cap, L, &c.d_cnt[CNT_ERR]);
+  // overflow fallback: returns at once unless the edge buffer overflowed
+  k_ccl_all<<<vgrid, 256, 0, s>>>(geo, n, L, &c.d_cnt[CNT_EDGES], st->edge_cap,
+                                  &c.d_cnt[CNT_ERR]);
+  k_resolve<<<vgrid, 256, 0, s>>>(d, st->code, st->nxt, L, key, keylist, c.d_cnt);
+  k_flood_seed<<<tiles, TX * TY, 0, s>>>(geo, st->code, key, L, ulist, c.d_cnt);
   const unsigned fgrid = grid_for(n, 256, c.sm_count, 4);
-  k_flood_layer2<<<fgrid, 256, 0, s>>>(d, st->code, key, ulist, &c.d_cnt[CNT_FRONT_SPARE], f0,
-                                       &c.d_cnt[CNT_FRONT0]); ++c.launches;
+  k_flood_layer2<<<fgrid, 256, 0, s>>>(geo, st->code, key, ulist, &c.d_cnt[CNT_FRONT_SPARE], f0,
+                                       &c.d_cnt[CNT_FRONT0]);
+  c.launches += 5;
   PNM_CUDA(cudaGetLastError());
 
-  // deeper layers, in batches of sweeps between host checks (empty sweeps are no-ops)
-  int* fin = f0;
-  int* fout = f1;
-  int cin = CNT_FRONT0, cout = CNT_FRONT1;
-  const int kBatch = 4, kMaxSweeps = 1 << 20;
-  int sweeps = 1;
-  while (true) {
-    for (int b = 0; b < kBatch; ++b) {
-      PNM_CUDA(cudaMemsetAsync(&c.d_cnt[cout], 0, sizeof(unsigned), s));
-      k_flood_assign<<<fgrid, 256, 0, s>>>(d, key, fin, &c.d_cnt[cin], tmp); ++c.launches;
-      k_flood_discover<<<fgrid, 256, 0, s>>>(d, st->code, key, L, fin, &c.d_cnt[cin], tmp, fout,
-                                             &c.d_cnt[cout]); ++c.launches;
-      std::swap(fin, fout);
-      std::swap(cin, cout);
-      ++sweeps;
+  // deeper layers: the persistent loop; if a cooperative launch is refused, the same sweeps as
+  // separate launches in batches between host checks (empty sweeps are no-ops)
+  const int kMaxSweeps = 1 << 20;
+  cudaError_t le = launch_flood_loop(geo, st->code, key, L, f0, f1, tmp, c.d_cnt, kMaxSweeps,
+                                     c.sm_count, n, s);
+  ++c.launches;
+  if (le != cudaSuccess) {
+    cudaGetLastError();
+    int* fin = f0;
+    int* fout = f1;
+    int cin = CNT_FRONT0, cout = CNT_FRONT1;
+    const int kBatch = 4;
+    int sweeps = 1;
+    while (true) {
+      for (int b = 0; b < kBatch; ++b) {
+        PNM_CUDA(cudaMemsetAsync(&c.d_cnt[cout], 0, sizeof(unsigned), s));
+        k_flood_assign<<<fgrid, 256, 0, s>>>(geo, key, fin, &c.d_cnt[cin], tmp);
+        k_flood_discover<<<fgrid, 256, 0, s>>>(geo, st->code, key, L, fin, &c.d_cnt[cin], tmp,
+                                               fout, &c.d_cnt[cout]);
+        c.launches += 2;
+        std::swap(fin, fout);
+        std::swap(cin, cout);
+        ++sweeps;
+      }
+      PNM_CUDA(cudaGetLastError());
+      PNM_TRY(c.read_counters());
+      if (c.h_cnt[cin] == 0) break;
+      if (sweeps > kMaxSweeps) return Status{PNM_ERR_NOT_CONVERGED, "flood did not converge"};
     }
-    PNM_CUDA(cudaGetLastError());
-    PNM_TRY(c.read_counters());
-    if (c.h_cnt[cin] == 0) break;
-    if (sweeps > kMaxSweeps) return Status{PNM_ERR_NOT_CONVERGED, "flood did not converge"};
+    st->flood_sweeps = sweeps;
   }
-  st->flood_sweeps = sweeps;
 
   // renumbering
   uint32_t *firstP, *firstS;
@@ -862,22 +1108,28 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   PNM_TRY(c.buf(S_SCAN0, words / SCAN_TILE + 2, &scan0));
   PNM_CUDA(cudaMemsetAsync(firstP, 0, words * 4, s));
   PNM_CUDA(cudaMemsetAsync(firstS, 0, words * 4, s));
-  const unsigned nkeys = c.h_cnt[CNT_KEYS];
-  const unsigned kgrid = grid_for(nkeys, 256, c.sm_count);
-  k_key_first<<<kgrid, 256, 0, s>>>(keylist, &c.d_cnt[CNT_KEYS], L, st->code, firstP, firstS); ++c.launches;
+  const unsigned kgrid = grid_for(n / 16 + 1, 256, c.sm_count);  // grid-stride over the keys
+  k_key_first<<<kgrid, 256, 0, s>>>(keylist, &c.d_cnt[CNT_KEYS], L, st->code, firstP, firstS);
   exclusive_scan(PopcountOf{firstP}, words, prefP, scan0, s, &c.launches);
   exclusive_scan(PopcountOf{firstS}, words, prefS, scan0, s, &c.launches);
-  k_key_id<<<kgrid, 256, 0, s>>>(keylist, &c.d_cnt[CNT_KEYS], L, st->code, firstP, prefP, firstS,
-                                 prefS); ++c.launches;
+  k_key_id<<<kgrid, 256, 0, s>>>(geo, keylist, &c.d_cnt[CNT_KEYS], L, st->code, firstP, prefP,
+                                 firstS, prefS);
+  c.launches += 2;
   PNM_CUDA(cudaGetLastError());
   unsigned tot[2];
   PNM_CUDA(cudaMemcpyAsync(&tot[0], prefP + words, 4, cudaMemcpyDeviceToHost, s));
   PNM_CUDA(cudaMemcpyAsync(&tot[1], prefS + words, 4, cudaMemcpyDeviceToHost, s));
-  PNM_CUDA(cudaStreamSynchronize(s));
+  PNM_TRY(c.read_counters());
   st->n_pore_labels = (int)tot[0];
   st->n_solid_labels = (int)tot[1];
+  st->n_edges = c.h_cnt[CNT_EDGES];
+  if (le == cudaSuccess) st->flood_sweeps = (int)c.h_cnt[CNT_SWEEPS];
   if (c.h_cnt[CNT_ERR] & ERRF_UF_LIMIT)
     return Status{PNM_ERR_NOT_CONVERGED, "union-find exceeded its iteration limit"};
+  if (c.h_cnt[CNT_ERR] & ERRF_FLOOD_LIMIT)
+    return Status{PNM_ERR_NOT_CONVERGED, "flood did not converge"};
+  if (c.h_cnt[CNT_ERR] & ERRF_BARRIER)
+    return Status{PNM_ERR_INTERNAL, "persistent flood loop: grid barrier timed out"};
   return Status::ok();
 }
 
@@ -899,14 +1151,14 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
     PNM_CUDA(cudaMemcpyAsync(range, init, sizeof(init), cudaMemcpyHostToDevice, s));
     PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_ERR], 0, sizeof(unsigned), s));
     PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_FLOW_SPARE1], 0, sizeof(unsigned), s));
-    const dim3 g((unsigned)((d.nx + STX - 1) / STX), (unsigned)((d.ny + STY - 1) / STY),
-                 (unsigned)((d.nz + STZ - 1) / STZ));
+    const unsigned g = (unsigned)boxes_of(d, STX, STY, STZ);
+    const OneVol geo{d, 0.0f};
     if (from_keys)
-      k_seg_topo<<<g, STX * STY, 0, s>>>(d, KeyLabels{st->key, st->idtab}, d_seg_out,
+      k_seg_topo<<<g, STX * STY, 0, s>>>(geo, KeyLabels{st->key, st->idtab}, d_seg_out,
                                          want_pairs ? 1 : 0, table, (uint64_t)(cap - 1), c.d_cnt,
                                          range);
     else
-      k_seg_topo<<<g, STX * STY, 0, s>>>(d, SegLabels{d_seg_in}, d_seg_out, want_pairs ? 1 : 0,
+      k_seg_topo<<<g, STX * STY, 0, s>>>(geo, SegLabels{d_seg_in}, d_seg_out, want_pairs ? 1 : 0,
                                          table, (uint64_t)(cap - 1), c.d_cnt, range);
     ++c.launches;
     PNM_CUDA(cudaGetLastError());
@@ -975,6 +1227,68 @@ Status run_pores(Ctx& c, const SegState& st, const float origin[3], const float 
   PNM_CUDA(cudaMemcpyAsync(&tot, pref + words, 4, cudaMemcpyDeviceToHost, s));
   PNM_CUDA(cudaStreamSynchronize(s));
   *n_pores = tot;
+  return Status::ok();
+}
+
+Status enqueue_batch(BatchPlan& p, cudaStream_t s, long long* launches) {
+  const long long n = p.n_total, words = p.words;
+  const int sm = p.sm_count;
+  const VolTab geo{p.vols, p.res, p.nvol};
+  PNM_CUDA(cudaMemsetAsync(p.cnt, 0, CNT_COUNT * sizeof(unsigned), s));
+  PNM_CUDA(cudaMemsetAsync(p.peakbits, 0, words * sizeof(uint32_t), s));
+  PNM_CUDA(cudaMemsetAsync(p.firstP, 0, words * sizeof(uint32_t), s));
+  PNM_CUDA(cudaMemsetAsync(p.firstS, 0, words * sizeof(uint32_t), s));
+  PNM_CUDA(cudaMemsetAsync(p.table, 0xff, p.hash_cap * sizeof(unsigned long long), s));
+  k_batch_init<<<1, 1, 0, s>>>(p.range);
+  const EdgeBuf eb{p.edges, p.edge_cap};
+  const unsigned vgrid = grid_for(n, 256, sm);
+  k_sdf_pass<false><<<(unsigned)p.tiles, TX * TY, 0, s>>>(p.sdf, geo, p.code, p.nxt, p.L,
+                                                          p.peakbits, eb, p.cnt);
+  k_ccl_edges<<<grid_for(n / 8 + 1, 256, sm), 256, 0, s>>>(p.edges, &p.cnt[CNT_EDGES], p.edge_cap,
+                                                           p.L, &p.cnt[CNT_ERR]);
+  k_ccl_all<<<vgrid, 256, 0, s>>>(geo, n, p.L, &p.cnt[CNT_EDGES], p.edge_cap, &p.cnt[CNT_ERR]);
+  k_resolve<<<vgrid, 256, 0, s>>>(Dims{(int)n, 1, 1}, p.code, p.nxt, p.L, p.key, p.keylist,
+                                  p.cnt);
+  k_flood_seed<<<(unsigned)p.tiles, TX * TY, 0, s>>>(geo, p.code, p.key, p.L, p.ulist, p.cnt);
+  k_flood_layer2<<<grid_for(n, 256, sm, 4), 256, 0, s>>>(
+      geo, p.code, p.key, p.ulist, &p.cnt[CNT_FRONT_SPARE], p.f0, &p.cnt[CNT_FRONT0]);
+  *launches += 7;
+  PNM_CUDA(cudaGetLastError());
+  PNM_CUDA(launch_flood_loop(geo, p.code, p.key, p.L, p.f0, p.f1, p.tmp, p.cnt, p.max_sweeps, sm,
+                             n, s, p.flood_blocks_per_sm));
+  const unsigned kgrid = grid_for(n / 16 + 1, 256, sm);
+  k_key_first<<<kgrid, 256, 0, s>>>(p.keylist, &p.cnt[CNT_KEYS], p.L, p.code, p.firstP, p.firstS);
+  exclusive_scan(PopcountOf{p.firstP}, words, p.prefP, p.scan_tmp, s, launches);
+  exclusive_scan(PopcountOf{p.firstS}, words, p.prefS, p.scan_tmp, s, launches);
+  k_key_id<<<kgrid, 256, 0, s>>>(geo, p.keylist, &p.cnt[CNT_KEYS], p.L, p.code, p.firstP,
+                                 p.prefP, p.firstS, p.prefS);
+  k_batch_labels<<<1, SCAN_THREADS, 0, s>>>(p.vols, p.res, p.nvol, p.prefP, p.prefS);
+  k_seg_topo<<<(unsigned)p.bricks, STX * STY, 0, s>>>(geo, KeyLabels{p.key, p.L}, p.seg, 1,
+                                                       p.table, (uint64_t)(p.hash_cap - 1), p.cnt,
+                                                       p.range);
+  *launches += 5;
+  PNM_CUDA(cudaGetLastError());
+  // unique pairs: compact the set, sort, decode per volume (counts stay on the device)
+  exclusive_scan(Occupied{p.table}, p.hash_cap, p.hpos, p.scan_tmp, s, launches);
+  const unsigned* m_p = p.hpos + p.hash_cap;
+  const unsigned hgrid = grid_for(p.hash_cap, 256, sm);
+  k_hash_gather<<<hgrid, 256, 0, s>>>(p.table, p.hash_cap, p.hpos, p.range, p.label_bits, p.ka);
+  p.pairs_in_b = radix_sort(p.ka, nullptr, p.kb, nullptr, p.hash_cap, 0, 2 * p.label_bits, p.hist,
+                            p.scan_tmp, s, launches, m_p);
+  const uint64_t* sorted = p.pairs_in_b ? p.kb : p.ka;
+  k_pairs_decode_batch<<<hgrid, 256, 0, s>>>(sorted, m_p, p.range, p.label_bits, geo, p.pairs);
+  // pores
+  exclusive_scan(PopcountOf{p.peakbits}, words, p.peakpref, p.scan_tmp, s, launches);
+  k_pores_emit_batch<<<grid_for(words, 256, sm), 256, 0, s>>>(p.sdf, geo, p.peakbits, p.peakpref,
+                                                              words, p.pores, p.pore_cap);
+  k_batch_tail<<<(unsigned)((p.nvol + 255) / 256), 256, 0, s>>>(
+      p.vols, p.res, p.nvol, p.peakpref, words, sorted, m_p, p.range, p.label_bits, p.cnt);
+  *launches += 4;
+  PNM_CUDA(cudaGetLastError());
+  PNM_CUDA(cudaMemcpyAsync(p.h_cnt, p.cnt, CNT_COUNT * sizeof(unsigned), cudaMemcpyDeviceToHost,
+                           s));
+  PNM_CUDA(cudaMemcpyAsync(p.h_res, p.res, p.nvol * sizeof(VolResult), cudaMemcpyDeviceToHost,
+                           s));
   return Status::ok();
 }
 
