@@ -198,7 +198,8 @@ void pnm_batch_destroy(pnm_batch* b);
 const char* pnm_batch_last_error(const pnm_batch* b);
 /* The batch's CUDA stream (cudaStream_t); every batch call is ordered on it. */
 void* pnm_batch_stream(const pnm_batch* b);
-/* Copies volume i's SDF (float32, x fastest) from host memory into the batch (async). */
+/* Copies volume i's SDF (float32, x fastest) into the batch, from host or device memory (async
+   on the batch stream; a device source must stay valid until the copy has run). */
 int pnm_batch_set_sdf(pnm_batch* b, int32_t i, const float* sdf);
 /* The batch SDF buffer on the device (volume i at voxel_offset) and its length in floats. */
 int pnm_batch_sdf_dev(pnm_batch* b, float** d_sdf, int64_t* n);

@@ -428,7 +428,7 @@ int pnm_batch_set_sdf(pnm_batch* b, int32_t i, const float* sdf) {
   auto body = [&]() -> Status {
     PNM_CUDA(cudaSetDevice(b->device));
     PNM_CUDA(cudaMemcpyAsync(const_cast<float*>(b->plan.sdf) + v.off, sdf, n * sizeof(float),
-                             cudaMemcpyHostToDevice, b->stream));
+                             cudaMemcpyDefault, b->stream));  // host or device source
     return Status::ok();
   };
   return fail(b, body());
