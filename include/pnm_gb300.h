@@ -219,6 +219,65 @@ int pnm_batch_get_stats(const pnm_batch* b, pnm_stats* out);
 /* 1 if runs replay a CUDA graph, 0 if they enqueue the stages (flag, or capture unavailable). */
 int pnm_batch_uses_graph(const pnm_batch* b);
 
+/* ---- serving ----------------------------------------------------------------------------
+ * No counterpart in the reference (its calls are serial and blocking, src/pnm_bindings.cpp:143).
+ * A request loop over batches: every request (one periodic volume) is queued on submit and
+ * admitted while the device-memory budget allows; requests queued when a stream slot frees are
+ * coalesced into one batch (continuous batching: arrivals during a run join the next batch), up
+ * to max_inflight batches run concurrently on their own streams, and each request's labels,
+ * pores and pairs stay resident on the device until it is released. The SDF passed to submit
+ * (host or device memory) must stay valid until the request is done or cancelled. */
+typedef struct pnm_server pnm_server;
+
+typedef struct {
+  int64_t budget_bytes;      /* device bytes for running batches and held results; 0: 120 GB */
+  int32_t max_inflight;      /* batches running at once, one stream each; 0: 3 */
+  int32_t max_batch_volumes; /* requests per batch; 0: 64 */
+  int64_t max_batch_voxels;  /* voxels per batch (a larger request runs alone); 0: 2^28 */
+  int32_t reserved[4];
+} pnm_server_config;
+
+typedef struct {
+  int64_t submitted, completed, failed, cancelled;
+  int64_t queued, running;   /* now */
+  int64_t batches;           /* batches launched */
+  int64_t bytes_in_use;      /* now: running batches + held results */
+  int64_t peak_bytes;
+  int64_t voxels_completed;
+  double p50_ms, p99_ms, mean_ms, max_ms; /* submit -> results resident, completed requests */
+  double busy_s;             /* first submit -> last completion */
+  double gvoxel_per_s;       /* voxels_completed / busy_s / 1e9 */
+} pnm_server_stats;
+
+#define PNM_REQ_QUEUED 0
+#define PNM_REQ_RUNNING 1
+#define PNM_REQ_DONE 2
+#define PNM_REQ_FAILED 3
+#define PNM_REQ_CANCELLED 4
+
+int pnm_server_create(pnm_ctx* ctx, const pnm_server_config* cfg, pnm_server** out);
+/* Fails queued requests as cancelled, waits for running batches, frees everything. */
+void pnm_server_destroy(pnm_server* s);
+const char* pnm_server_last_error(const pnm_server* s);
+int pnm_server_submit(pnm_server* s, const float* sdf, int32_t nx, int32_t ny, int32_t nz,
+                      const float origin_xyz[3], const float spacing_xyz[3], int64_t* ticket);
+/* state: PNM_REQ_*; status: the request's PNM_* result once done or failed. */
+int pnm_server_state(pnm_server* s, int64_t ticket, int32_t* state, int32_t* status);
+/* Blocks until the request is done, failed or cancelled; returns its status
+   (PNM_ERR_NOT_CONVERGED if timeout_s > 0 passes first). */
+int pnm_server_wait(pnm_server* s, int64_t ticket, double timeout_s);
+/* Removes a queued request (PNM_ERR_ARG once it is running or finished). */
+int pnm_server_cancel(pnm_server* s, int64_t ticket);
+/* Counts (info) and device pointers of a done request's resident results (any may be null). */
+int pnm_server_result(pnm_server* s, int64_t ticket, pnm_batch_volume* info, pnm_pore** d_pores,
+                      int32_t** d_seg, int32_t** d_pairs);
+int pnm_server_copy_out(pnm_server* s, int64_t ticket, pnm_pore* pores, int32_t* seg,
+                        int32_t* pairs);
+/* Drops a finished request (its batch's memory returns when all its requests are released). */
+int pnm_server_release(pnm_server* s, int64_t ticket);
+int pnm_server_get_stats(pnm_server* s, pnm_server_stats* out);
+int pnm_server_reset_stats(pnm_server* s);
+
 #ifdef __cplusplus
 }
 #endif

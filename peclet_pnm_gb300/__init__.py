@@ -27,11 +27,12 @@ from ._capi import Context, PnmError, default_context
 
 __all__ = ["Pore", "extract_pores", "segment_volume", "extract_topology_gpu",
            "extract_pore_network", "extract_network_flow", "execution_space", "Context",
-           "PnmError", "Batch", "extract_pore_network_batch", "batch_plan_bytes"]
+           "PnmError", "Batch", "extract_pore_network_batch", "batch_plan_bytes", "Server"]
 
 execution_space = _capi.pnm_execution_space().decode()
 
 from .batch import Batch, batch_plan_bytes, extract_pore_network_batch  # noqa: E402
+from .server import Server  # noqa: E402
 
 
 class Pore:

@@ -119,6 +119,38 @@ pnm_batch_copy_out = _sig("pnm_batch_copy_out", ctypes.c_int, _vp, _i32, _vp, _v
 pnm_batch_get_stats = _sig("pnm_batch_get_stats", ctypes.c_int, _vp, _P(PnmStats))
 pnm_batch_uses_graph = _sig("pnm_batch_uses_graph", ctypes.c_int, _vp)
 
+
+
+class PnmServerConfig(ctypes.Structure):
+    _fields_ = [("budget_bytes", _i64), ("max_inflight", _i32), ("max_batch_volumes", _i32),
+                ("max_batch_voxels", _i64), ("reserved", _i32 * 4)]
+
+
+class PnmServerStats(ctypes.Structure):
+    _fields_ = [("submitted", _i64), ("completed", _i64), ("failed", _i64), ("cancelled", _i64),
+                ("queued", _i64), ("running", _i64), ("batches", _i64), ("bytes_in_use", _i64),
+                ("peak_bytes", _i64), ("voxels_completed", _i64), ("p50_ms", ctypes.c_double),
+                ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
+                ("max_ms", ctypes.c_double), ("busy_s", ctypes.c_double),
+                ("gvoxel_per_s", ctypes.c_double)]
+
+
+PNM_REQ_QUEUED, PNM_REQ_RUNNING, PNM_REQ_DONE, PNM_REQ_FAILED, PNM_REQ_CANCELLED = range(5)
+pnm_server_create = _sig("pnm_server_create", ctypes.c_int, _vp, _P(PnmServerConfig), _P(_vp))
+pnm_server_destroy = _sig("pnm_server_destroy", None, _vp)
+pnm_server_last_error = _sig("pnm_server_last_error", ctypes.c_char_p, _vp)
+pnm_server_submit = _sig("pnm_server_submit", ctypes.c_int, _vp, _vp, _i32, _i32, _i32, _vp, _vp,
+                         _P(_i64))
+pnm_server_state = _sig("pnm_server_state", ctypes.c_int, _vp, _i64, _P(_i32), _P(_i32))
+pnm_server_wait = _sig("pnm_server_wait", ctypes.c_int, _vp, _i64, ctypes.c_double)
+pnm_server_cancel = _sig("pnm_server_cancel", ctypes.c_int, _vp, _i64)
+pnm_server_result = _sig("pnm_server_result", ctypes.c_int, _vp, _i64, _P(PnmBatchVolume),
+                         _P(_vp), _P(_vp), _P(_vp))
+pnm_server_copy_out = _sig("pnm_server_copy_out", ctypes.c_int, _vp, _i64, _vp, _vp, _vp)
+pnm_server_release = _sig("pnm_server_release", ctypes.c_int, _vp, _i64)
+pnm_server_get_stats = _sig("pnm_server_get_stats", ctypes.c_int, _vp, _P(PnmServerStats))
+pnm_server_reset_stats = _sig("pnm_server_reset_stats", ctypes.c_int, _vp)
+
 #: every symbol include/pnm_gb300.h declares
 EXPORTED = ["pnm_ctx_create", "pnm_ctx_destroy", "pnm_last_error", "pnm_ctx_set_stream",
             "pnm_ctx_trim", "pnm_execution_space", "pnm_free", "pnm_extract_pores",
@@ -129,7 +161,10 @@ EXPORTED = ["pnm_ctx_create", "pnm_ctx_destroy", "pnm_last_error", "pnm_ctx_set_
             "pnm_batch_last_error", "pnm_batch_stream", "pnm_batch_set_sdf", "pnm_batch_sdf_dev",
             "pnm_batch_launch", "pnm_batch_wait", "pnm_batch_run", "pnm_batch_volume_info",
             "pnm_batch_results_dev", "pnm_batch_copy_out", "pnm_batch_get_stats",
-            "pnm_batch_uses_graph"]
+            "pnm_batch_uses_graph", "pnm_server_create", "pnm_server_destroy",
+            "pnm_server_last_error", "pnm_server_submit", "pnm_server_state", "pnm_server_wait",
+            "pnm_server_cancel", "pnm_server_result", "pnm_server_copy_out", "pnm_server_release",
+            "pnm_server_get_stats", "pnm_server_reset_stats"]
 
 
 class PnmError(RuntimeError):

@@ -19,7 +19,8 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 OBJDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpnm_gb300.so")
-SOURCES = ["pnm_segment.cu", "pnm_flow.cu", "pnm_capi.cu", "pnm_noalloc.cu", "pnm_batch.cu"]
+SOURCES = ["pnm_segment.cu", "pnm_flow.cu", "pnm_capi.cu", "pnm_noalloc.cu", "pnm_batch.cu",
+           "pnm_server.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no floating-point contraction anywhere (float centroids and the float64

@@ -136,6 +136,8 @@ struct pnm_batch {
   void* pairbuf = nullptr;
   void* porebuf = nullptr;
   void* pinned = nullptr;
+  bool own_stream = true;
+  bool own_pinned = true;
   bool use_graph = true;
   cudaGraphExec_t exec = nullptr;
   long long launches_per_run = 0;
@@ -230,14 +232,14 @@ Status regrow(pnm_batch& b, long long hash_cap, long long pore_cap) {
   PNM_CUDA(cudaStreamSynchronize(b.stream));
   drop_graph(b);
   if (L.pairbuf != b.lay.pairbuf) {
-    cudaFree(b.pairbuf);
+    cudaFreeAsync(b.pairbuf, b.stream);
     b.pairbuf = nullptr;
-    PNM_CUDA(cudaMalloc(&b.pairbuf, L.pairbuf));
+    PNM_CUDA(cudaMallocAsync(&b.pairbuf, L.pairbuf, b.stream));
   }
   if (L.porebuf != b.lay.porebuf) {
-    cudaFree(b.porebuf);
+    cudaFreeAsync(b.porebuf, b.stream);
     b.porebuf = nullptr;
-    PNM_CUDA(cudaMalloc(&b.porebuf, L.porebuf));
+    PNM_CUDA(cudaMallocAsync(&b.porebuf, L.porebuf, b.stream));
   }
   L.arena = b.lay.arena;  // unchanged sizes (the scan partials were sized for the first hash cap)
   const long long W = L.words, hc = L.hash_cap;
@@ -252,11 +254,10 @@ Status regrow(pnm_batch& b, long long hash_cap, long long pore_cap) {
                              &full));
     const size_t sdf_bytes = (size_t)b.lay.n_total * 4;
     void* na = nullptr;
-    PNM_CUDA(cudaMalloc(&na, full.arena));
+    PNM_CUDA(cudaMallocAsync(&na, full.arena, b.stream));
     // the SDF lives at the start of the arena: keep it across the move
     PNM_CUDA(cudaMemcpyAsync(na, b.plan.sdf, sdf_bytes, cudaMemcpyDeviceToDevice, b.stream));
-    PNM_CUDA(cudaStreamSynchronize(b.stream));
-    cudaFree(b.arena);
+    cudaFreeAsync(b.arena, b.stream);
     b.arena = na;
     L.arena = full.arena;
   }
@@ -356,6 +357,72 @@ int fail(pnm_batch* b, Status s) {
 
 }  // namespace
 
+namespace pnm {
+
+// Keeps freed batch memory in the device's default pool (stream-ordered allocations are then
+// served from it), once per process and device.
+void keep_pool(int device) {
+  static bool done[64] = {};
+  if (device < 0 || device >= 64 || done[device]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    unsigned long long thr = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  cudaGetLastError();
+  done[device] = true;
+}
+
+Status batch_new(int device, int sm_count, cudaStream_t stream, void* pinned, int flags, int nvol,
+                 const int32_t* dims_xyz, const float* origin_xyz, const float* spacing_xyz,
+                 pnm_batch** out) {
+  *out = nullptr;
+  auto* b = new (std::nothrow) pnm_batch();
+  if (!b) return Status{PNM_ERR_INTERNAL, "out of host memory"};
+  auto body = [&]() -> Status {
+    b->device = device;
+    b->sm_count = sm_count;
+    b->use_graph = !(flags & PNM_BATCH_NO_GRAPH);
+    PNM_TRY(make_layout(nvol, dims_xyz, origin_xyz, spacing_xyz, 0, 0, &b->lay));
+    PNM_CUDA(cudaSetDevice(device));
+    keep_pool(device);
+    if (stream) {
+      b->stream = stream;
+      b->own_stream = false;
+    } else {
+      PNM_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    }
+    PNM_CUDA(cudaMallocAsync(&b->arena, b->lay.arena, b->stream));
+    PNM_CUDA(cudaMallocAsync(&b->pairbuf, b->lay.pairbuf, b->stream));
+    PNM_CUDA(cudaMallocAsync(&b->porebuf, b->lay.porebuf, b->stream));
+    const size_t pin_bytes = 256 + nvol * sizeof(VolResult);
+    if (pinned) {
+      b->pinned = pinned;
+      b->own_pinned = false;
+    } else {
+      PNM_CUDA(cudaMallocHost(&b->pinned, pin_bytes));
+    }
+    std::memset(b->pinned, 0, pin_bytes);
+    PNM_TRY(carve(*b));
+    PNM_CUDA(cudaMemcpyAsync(const_cast<VolDesc*>(b->plan.vols), b->lay.vols.data(),
+                             nvol * sizeof(VolDesc), cudaMemcpyHostToDevice, b->stream));
+    PNM_CUDA(cudaMemsetAsync(b->plan.res, 0, nvol * sizeof(VolResult), b->stream));
+    return Status::ok();
+  };
+  Status s = body();
+  if (!s.good()) {
+    cudaGetLastError();
+    pnm_batch_destroy(b);
+    return s;
+  }
+  *out = b;
+  return Status::ok();
+}
+
+size_t batch_pinned_bytes(int nvol) { return 256 + (size_t)nvol * sizeof(VolResult); }
+
+}  // namespace pnm
+
 extern "C" {
 
 int pnm_batch_plan_bytes(int32_t n_volumes, const int32_t* dims_xyz, int64_t* bytes) {
@@ -372,47 +439,25 @@ int pnm_batch_create(pnm_ctx* ctx, int32_t n_volumes, const int32_t* dims_xyz,
                      pnm_batch** out) {
   if (!ctx || !out || !origin_xyz || !spacing_xyz) return PNM_ERR_ARG;
   *out = nullptr;
-  auto* b = new (std::nothrow) pnm_batch();
-  if (!b) return PNM_ERR_INTERNAL;
-  auto body = [&]() -> Status {
-    b->device = ctx->c.device;
-    b->sm_count = ctx->c.sm_count;
-    b->use_graph = !(flags & PNM_BATCH_NO_GRAPH);
-    PNM_TRY(pnm::make_layout(n_volumes, dims_xyz, origin_xyz, spacing_xyz, 0, 0, &b->lay));
-    PNM_CUDA(cudaSetDevice(b->device));
-    PNM_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
-    PNM_CUDA(cudaMalloc(&b->arena, b->lay.arena));
-    PNM_CUDA(cudaMalloc(&b->pairbuf, b->lay.pairbuf));
-    PNM_CUDA(cudaMalloc(&b->porebuf, b->lay.porebuf));
-    PNM_CUDA(cudaMallocHost(&b->pinned, 256 + n_volumes * sizeof(pnm::VolResult)));
-    PNM_TRY(carve(*b));
-    PNM_CUDA(cudaMemcpy(const_cast<pnm::VolDesc*>(b->plan.vols), b->lay.vols.data(),
-                        n_volumes * sizeof(pnm::VolDesc), cudaMemcpyHostToDevice));
-    PNM_CUDA(cudaMemset(b->plan.res, 0, n_volumes * sizeof(pnm::VolResult)));
-    std::memset(b->pinned, 0, 256 + n_volumes * sizeof(pnm::VolResult));
-    return Status::ok();
-  };
-  Status s = body();
-  if (!s.good()) {
-    ctx->c.last_error = s.msg;
-    cudaGetLastError();
-    pnm_batch_destroy(b);
-    return s.code;
-  }
-  *out = b;
-  return PNM_OK;
+  Status s = pnm::batch_new(ctx->c.device, ctx->c.sm_count, nullptr, nullptr, flags, n_volumes,
+                            dims_xyz, origin_xyz, spacing_xyz, out);
+  if (!s.good()) ctx->c.last_error = s.msg;
+  return s.code;
 }
 
 void pnm_batch_destroy(pnm_batch* b) {
   if (!b) return;
   cudaSetDevice(b->device);
-  if (b->stream) cudaStreamSynchronize(b->stream);
+  // pending copies into host mirrors this batch owns; a borrowed stream may already carry other
+  // work, and the stream-ordered frees below need no wait
+  if (b->stream && (b->own_pinned || b->own_stream)) cudaStreamSynchronize(b->stream);
   drop_graph(*b);
-  if (b->arena) cudaFree(b->arena);
-  if (b->pairbuf) cudaFree(b->pairbuf);
-  if (b->porebuf) cudaFree(b->porebuf);
-  if (b->pinned) cudaFreeHost(b->pinned);
-  if (b->stream) cudaStreamDestroy(b->stream);
+  // stream-ordered frees: no device-wide synchronisation, memory goes back to the pool
+  if (b->arena) cudaFreeAsync(b->arena, b->stream);
+  if (b->pairbuf) cudaFreeAsync(b->pairbuf, b->stream);
+  if (b->porebuf) cudaFreeAsync(b->porebuf, b->stream);
+  if (b->pinned && b->own_pinned) cudaFreeHost(b->pinned);
+  if (b->stream && b->own_stream) cudaStreamDestroy(b->stream);
   delete b;
 }
 

@@ -173,6 +173,17 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
 
 }  // namespace pnm
 
+// ---- batches (pnm_batch.cu) ---------------------------------------------------------------------
+namespace pnm {
+// Plans and allocates a batch (stream-ordered allocations on `stream`; null: the batch creates
+// and owns a stream). `pinned` (optional, batch_pinned_bytes(nvol)) receives the per-run
+// figures; null: the batch allocates its own.
+Status batch_new(int device, int sm_count, cudaStream_t stream, void* pinned, int flags, int nvol,
+                 const int32_t* dims_xyz, const float* origin_xyz, const float* spacing_xyz,
+                 pnm_batch** out);
+size_t batch_pinned_bytes(int nvol);
+}  // namespace pnm
+
 // The opaque handle of the C ABI.
 struct pnm_ctx {
   pnm::Ctx c;
