@@ -53,6 +53,12 @@ def parse():
     ap.add_argument("--ref-sample", type=int, default=256,
                     help="cube edge of one reference-arm step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the ragged 96-volume batched-vs-plain measurement")
+    ap.add_argument("--no-served", action="store_true",
+                    help="skip the Poisson serving measurement")
+    ap.add_argument("--batch-volumes", type=int, default=96)
+    ap.add_argument("--serve-requests", type=int, default=600)
     return ap.parse_args()
 
 
@@ -186,6 +192,255 @@ def reference_arm(args, rank):
                 "d2h_bytes_per_step": 0}}), flush=True)
 
 
+def batched_bench(args, dev):
+    """Ragged batch: 96 packings, edges drawn per axis from {48,...,192} (seed 5+i), porosity
+    U[0.3,0.6]. Batched (one launch per stage, graph replay) vs the plain per-volume path in a loop,
+    both with the SDFs resident; e2e adds the H2D of every SDF from pinned memory and the D2H of
+    every result (labels, pores, pairs)."""
+    import torch
+
+    import peclet_pnm_gb300 as pnm
+    from peclet_pnm_gb300 import _capi
+    from peclet_pnm_gb300 import synthetic as syn
+
+    shapes = syn.batch_shapes(args.batch_volumes)
+    vols = [syn.packing(sh, phi, seed=sd, device=dev) for sh, phi, sd in shapes]
+    torch.cuda.synchronize(dev)
+    nvox = sum(int(v.numel()) for v in vols)
+    ctx = pnm.Context(dev.index)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    o = np.zeros(3, np.float32)
+    s = np.ones(3, np.float32)
+    maxn = max(int(v.numel()) for v in vols)
+    d_seg = torch.empty(maxn, dtype=torch.int32, device=dev)
+    d_pores = torch.empty((1_000_000, 4), dtype=torch.float32, device=dev)
+    pair_cap = 8_000_000
+    d_pairs = torch.empty((pair_cap, 2), dtype=torch.int32, device=dev)
+    npo, npa = _capi._i64(), _capi._i64()
+
+    def plain_all():
+        for v in vols:
+            nz, ny, nx = v.shape
+            ctx.check(_capi.pnm_extract_pore_network_dev(
+                ctx.h, v.data_ptr(), nx, ny, nz, _capi.as_ptr(o), _capi.as_ptr(s),
+                d_pores.data_ptr(), 1_000_000, ctypes.byref(npo), d_seg.data_ptr(),
+                d_pairs.data_ptr(), pair_cap, ctypes.byref(npa)))
+
+    for _ in range(args.warmup):
+        plain_all()
+    torch.cuda.synchronize(dev)
+    l0 = ctx.stats()["launches"]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        plain_all()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    plain_ms = e0.elapsed_time(e1) / args.steps
+    plain_launches = (ctx.stats()["launches"] - l0) // args.steps
+
+    b = pnm.Batch([tuple(v.shape) for v in vols])
+    for i, v in enumerate(vols):
+        b.check(_capi.pnm_batch_set_sdf(b.h, i, ctypes.c_void_p(v.data_ptr())))
+    bstream = torch.cuda.ExternalStream(b.stream, device=dev)
+    for _ in range(args.warmup):
+        b.run()
+    e0.record(bstream)
+    for _ in range(args.steps):
+        b.launch()
+        b.wait()
+    e1.record(bstream)
+    torch.cuda.synchronize(dev)
+    batch_ms = e0.elapsed_time(e1) / args.steps
+
+    # e2e: pinned host SDFs in, every volume's labels, pores and pairs out, each step
+    hs = [torch.empty(v.shape, dtype=torch.float32, pin_memory=True) for v in vols]
+    for h, v in zip(hs, vols):
+        h.copy_(v)
+    infos = [b.volume(i) for i in range(len(vols))]
+    tot_p = sum(v["n_pores"] for v in infos)
+    tot_q = sum(v["n_pairs"] for v in infos)
+    hseg = torch.empty(nvox + 1, dtype=torch.int32, pin_memory=True)
+    hpores = torch.empty(4 * tot_p + 4, dtype=torch.float32, pin_memory=True)
+    hpairs = torch.empty(2 * tot_q + 2, dtype=torch.int32, pin_memory=True)
+
+    def e2e_step():
+        for i, h in enumerate(hs):
+            b.check(_capi.pnm_batch_set_sdf(b.h, i, ctypes.c_void_p(h.data_ptr())))
+        b.run()
+        so = po = qo = 0
+        for i in range(len(hs)):
+            b.check(_capi.pnm_batch_copy_out(
+                b.h, i, ctypes.c_void_p(hpores.data_ptr() + 16 * po),
+                ctypes.c_void_p(hseg.data_ptr() + 4 * so),
+                ctypes.c_void_p(hpairs.data_ptr() + 8 * qo)))
+            so += infos[i]["nx"] * infos[i]["ny"] * infos[i]["nz"]
+            po += infos[i]["n_pores"]
+            qo += infos[i]["n_pairs"]
+        return 4 * so, 4 * so + 16 * po + 8 * qo
+
+    e2e_step()
+    t0 = time.perf_counter()
+    k = max(3, min(args.steps, 5))
+    for _ in range(k):
+        h2d, d2h = e2e_step()
+    t_e2e = (time.perf_counter() - t0) / k
+    st = b.stats()
+    out = {
+        "workload": f"{len(vols)} ragged float32 packings, edges per axis from "
+                    "{48,64,96,128,160,192}, porosity U[0.3,0.6], seeds 5+i",
+        "voxels": nvox,
+        "batched": {"value": nvox / (batch_ms * 1e-3) / 1e9, "unit": "Gvoxel/s",
+                    "ms_per_step": batch_ms, "gpu_launches": int(st["launches"]),
+                    "cuda_graph": b.uses_graph},
+        "plain": {"value": nvox / (plain_ms * 1e-3) / 1e9, "unit": "Gvoxel/s",
+                  "ms_per_step": plain_ms, "gpu_launches": int(plain_launches)},
+        "batched_over_plain": plain_ms / batch_ms,
+        "e2e": {"value": nvox / t_e2e / 1e9, "unit": "Gvoxel/s", "ms_per_step": t_e2e * 1e3,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "outputs": {"pores": int(st["n_pores"]), "pairs": int(st["n_pairs"]),
+                    "flood_sweeps": int(st["flood_sweeps"])},
+    }
+    b.close()
+    ctx.close()
+    del vols
+    torch.cuda.empty_cache()
+    return out
+
+
+def served_bench(args, dev):
+    """Poisson requests (rate 200/s, seed 6), cubic edges log-uniform in [32, 384], SDFs in pinned
+    host memory: 64 distinct request volumes cut from two 384^3 packings, cycled through the
+    stream. Latency = submit -> labels, pores and pairs resident on the device. The server
+    (continuous batching, 120 GB budget) against the plain per-request path (FIFO, one request
+    at a time: H2D + pnm_extract_pore_network_dev), each also under a saturating burst."""
+    import threading
+
+    import torch
+
+    import peclet_pnm_gb300 as pnm
+    from peclet_pnm_gb300 import _capi
+    from peclet_pnm_gb300 import synthetic as syn
+
+    rng = np.random.default_rng(6)
+    big = [syn.packing((384, 384, 384), 0.45, seed=60 + k, device=dev) for k in range(2)]
+    pool = []
+    for i in range(64):
+        e = int(round(np.exp(rng.uniform(np.log(32), np.log(384)))))
+        src = big[i % 2]
+        oz, oy, ox = (int(rng.integers(0, 385 - e)) for _ in range(3))
+        h = torch.empty((e, e, e), dtype=torch.float32, pin_memory=True)
+        h.copy_(src[oz:oz + e, oy:oy + e, ox:ox + e])
+        pool.append(h)
+    del big
+    torch.cuda.empty_cache()
+    n_req = args.serve_requests
+    arrivals = np.cumsum(rng.exponential(1.0 / 200.0, size=n_req))
+    reqs = [pool[j % len(pool)] for j in range(n_req)]
+    vox = sum(int(r.numel()) for r in reqs)
+
+    ctx = pnm.Context(dev.index)
+    stream = torch.cuda.Stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    maxn = max(int(r.numel()) for r in pool)
+    d_sdf = torch.empty(maxn, dtype=torch.float32, device=dev)
+    d_seg = torch.empty(maxn, dtype=torch.int32, device=dev)
+    d_pores = torch.empty((1_000_000, 4), dtype=torch.float32, device=dev)
+    d_pairs = torch.empty((8_000_000, 2), dtype=torch.int32, device=dev)
+    npo, npa = _capi._i64(), _capi._i64()
+    o = np.zeros(3, np.float32)
+    s = np.ones(3, np.float32)
+
+    def plain_one(h):
+        e = h.shape[0]
+        with torch.cuda.stream(stream):
+            d_sdf[:h.numel()].copy_(h.view(-1), non_blocking=True)
+        ctx.check(_capi.pnm_extract_pore_network_dev(
+            ctx.h, d_sdf.data_ptr(), e, e, e, _capi.as_ptr(o), _capi.as_ptr(s),
+            d_pores.data_ptr(), 1_000_000, ctypes.byref(npo), d_seg.data_ptr(),
+            d_pairs.data_ptr(), 8_000_000, ctypes.byref(npa)))
+        stream.synchronize()
+
+    for h in pool[:8]:
+        plain_one(h)
+    lat = []
+    t0 = time.perf_counter()
+    for j in range(n_req):
+        wait = arrivals[j] - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        plain_one(reqs[j])
+        lat.append(time.perf_counter() - t0 - arrivals[j])
+    plain_span = time.perf_counter() - t0
+    lat = np.array(lat) * 1e3
+    t0 = time.perf_counter()
+    for h in reqs[:200]:
+        plain_one(h)
+    plain_burst = sum(int(h.numel()) for h in reqs[:200]) / (time.perf_counter() - t0) / 1e9
+
+    srv = pnm.Server(max_inflight=2)
+    for t in [srv.submit(h) for h in pool[:8]]:
+        srv.wait(t)
+        srv.release(t)
+    srv.reset_stats()
+    tickets = []
+    errors = []
+
+    def reaper(n):
+        k = 0
+        while k < n:
+            if k >= len(tickets):
+                time.sleep(0.0002)
+                continue
+            rc = srv.wait(tickets[k])
+            if rc != 0:
+                errors.append(rc)
+            srv.release(tickets[k])
+            k += 1
+
+    th = threading.Thread(target=reaper, args=(n_req,))
+    th.start()
+    t0 = time.perf_counter()
+    for j in range(n_req):
+        wait = arrivals[j] - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        tickets.append(srv.submit(reqs[j]))
+    th.join()
+    sp = srv.stats()
+    srv.reset_stats()
+    tickets.clear()
+    th = threading.Thread(target=reaper, args=(200,))
+    th.start()
+    t0 = time.perf_counter()
+    for h in reqs[:200]:
+        tickets.append(srv.submit(h))
+    th.join()
+    burst_s = time.perf_counter() - t0
+    sb = srv.stats()
+    srv.close()
+    ctx.close()
+    if errors:
+        raise RuntimeError(f"served requests failed: {errors[:5]}")
+    burst_vox = sum(int(h.numel()) for h in reqs[:200])
+    return {
+        "workload": f"{n_req} Poisson requests at 200/s (seed 6), cubic edges log-uniform in "
+                    "[32,384], pinned host SDFs, 120 GB budget",
+        "offered_gvoxel_per_s": vox / arrivals[-1] / 1e9,
+        "served": {"p50_ms": sp["p50_ms"], "p99_ms": sp["p99_ms"], "mean_ms": sp["mean_ms"],
+                   "gvoxel_per_s": sp["gvoxel_per_s"], "batches": int(sp["batches"]),
+                   "requests": int(sp["completed"]),
+                   "peak_device_gb": sp["peak_bytes"] / 1e9},
+        "plain": {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                  "mean_ms": float(lat.mean()), "gvoxel_per_s": vox / plain_span / 1e9},
+        "burst_200": {"served_gvoxel_per_s": burst_vox / burst_s / 1e9,
+                      "served_batches": int(sb["batches"]),
+                      "served_p50_ms": sb["p50_ms"], "served_p99_ms": sb["p99_ms"],
+                      "plain_gvoxel_per_s": plain_burst},
+    }
+
+
 def ours(args, rank, world, local_rank):
     import torch
 
@@ -314,9 +569,15 @@ def ours(args, rank, world, local_rank):
             "kind": "port",
             "sample": f"{args.cpu_sample}^3 corner of the benchmark volume, one "
                       f"extract_pore_network ({t_cpu:.1f} s, C++ restatement with OpenMP)"}
+    ctx.close()
+    del sdf
+    torch.cuda.empty_cache()
+    if rank == 0 and world == 1 and not args.no_batched:
+        result["batched"] = batched_bench(args, dev)
+    if rank == 0 and world == 1 and not args.no_served:
+        result["served"] = served_bench(args, dev)
     if rank == 0:
         print(json.dumps(result), flush=True)
-    ctx.close()
 
 
 def main():
