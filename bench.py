@@ -138,6 +138,23 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def replica_seed(rank: int) -> int:
+    """Each rank extracts its own volume (replicas: the path does not shard one volume)."""
+    return 2 + rank
+
+
+def whole_job_rate(local_value: float, voxels_per_rank: int, world: int, device) -> tuple:
+    """(max over ranks of a per-rank step time, whole-job Gvoxel/s = all ranks' voxels / that
+    time). Rank timings are combined with an all-reduce MAX when a process group is up."""
+    import torch
+
+    t = torch.tensor([float(local_value)], dtype=torch.float64, device=device)
+    if world > 1 and torch.distributed.is_initialized():
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    worst = float(t.item())
+    return worst, voxels_per_rank * world / worst / 1e9
+
+
 def gen_volume(n_edge, seed, device):
     from peclet_pnm_gb300 import synthetic as syn
 
@@ -450,7 +467,7 @@ def ours(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     n_edge = args.size
-    sdf = gen_volume(n_edge, 2 + rank, dev)
+    sdf = gen_volume(n_edge, replica_seed(rank), dev)
     nvox = sdf.numel()
     ctx = pnm.Context(local_rank)
     stream = torch.cuda.current_stream(dev)
@@ -500,11 +517,8 @@ def ours(args, rank, world, local_rank):
     launches = ctx.stats()["launches"] - launches0
     ms = e0.elapsed_time(e1) / args.steps
     st = ctx.stats()
-    t = torch.tensor([ms], device=dev)
-    if dist:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = nvox * world / (ms_max * 1e-3) / 1e9
+    s_max, value = whole_job_rate(ms * 1e-3, nvox, world, dev)
+    ms_max = s_max * 1e3
 
     # e2e through the host C ABI from pinned memory
     h_sdf = torch.empty(sdf.shape, dtype=torch.float32, pin_memory=True)
@@ -532,10 +546,7 @@ def ours(args, rank, world, local_rank):
     for _ in range(k_e2e):
         e2e_step()
     t_e2e = (time.perf_counter() - t0) / k_e2e
-    te = torch.tensor([t_e2e], device=dev)
-    if dist:
-        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = nvox * world / float(te.item()) / 1e9
+    _, e2e_value = whole_job_rate(t_e2e, nvox, world, dev)
 
     peak, peak_src = measured_hbm_peak()
     achieved = ALG_BYTES_PER_VOXEL * nvox / (ms * 1e-3) / 1e9

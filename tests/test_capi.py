@@ -101,3 +101,36 @@ def test_product_never_imports_the_oracle():
                 text = open(os.path.join(dirpath, f)).read()
                 assert not re.search(r"^\s*(from|import)\s+oracle\b", text, re.M), f
                 assert "libpnm_oracle" not in text and "libpnm_ref" not in text, f
+
+
+def test_batch_planning_without_device():
+    """Batch layout and admission sizes are host arithmetic: 32-voxel-aligned volume offsets,
+    monotone plan bytes, and the reference binding's argument errors."""
+    import peclet_pnm_gb300 as pnm
+    from peclet_pnm_gb300 import _capi
+
+    small = pnm.batch_plan_bytes([(8, 8, 8)])
+    two = pnm.batch_plan_bytes([(8, 8, 8), (9, 7, 5)])
+    big = pnm.batch_plan_bytes([(64, 64, 64)])
+    assert 0 < small < two < big
+    # about 50 device bytes per voxel once the fixed parts are amortised
+    per_voxel = (pnm.batch_plan_bytes([(256, 256, 256)]) - big) / (256 ** 3 - 64 ** 3)
+    assert 30 < per_voxel < 80
+    d = np.array([[4, 4, -1]], np.int32)
+    out = _capi._i64()
+    assert _capi.pnm_batch_plan_bytes(1, _capi.as_ptr(d), ctypes.byref(out)) == _capi.PNM_ERR_ARG
+    d = np.array([[2048, 2048, 1024]], np.int32)
+    assert _capi.pnm_batch_plan_bytes(1, _capi.as_ptr(d), ctypes.byref(out)) == \
+        _capi.PNM_ERR_SHAPE
+    assert _capi.pnm_batch_plan_bytes(0, None, ctypes.byref(out)) == _capi.PNM_ERR_ARG
+    h = ctypes.c_void_p()
+    dims = np.array([[4, 4, 4]], np.int32)
+    f = np.zeros(3, np.float32)
+    assert _capi.pnm_batch_create(None, 1, _capi.as_ptr(dims), _capi.as_ptr(f), _capi.as_ptr(f),
+                                  0, ctypes.byref(h)) == _capi.PNM_ERR_ARG
+    assert _capi.pnm_server_create(None, None, ctypes.byref(h)) == _capi.PNM_ERR_ARG
+    t = _capi._i64()
+    assert _capi.pnm_server_submit(None, None, 1, 1, 1, _capi.as_ptr(f), _capi.as_ptr(f),
+                                   ctypes.byref(t)) == _capi.PNM_ERR_ARG
+    assert _capi.pnm_batch_run(None) == _capi.PNM_ERR_ARG
+    assert _capi.pnm_server_wait(None, 1, 0.0) == _capi.PNM_ERR_ARG
