@@ -260,6 +260,10 @@ def batched_bench(args, dev):
     b = pnm.Batch([tuple(v.shape) for v in vols])
     for i, v in enumerate(vols):
         b.check(_capi.pnm_batch_set_sdf(b.h, i, ctypes.c_void_p(v.data_ptr())))
+    # launch shape for this size class (timed on this data; not part of the timed region)
+    t_tune = time.perf_counter()
+    tuned = b.autotune(cache=os.path.join(tempfile.mkdtemp(), "tune.txt"), reps=2)
+    t_tune = time.perf_counter() - t_tune
     bstream = torch.cuda.ExternalStream(b.stream, device=dev)
     for _ in range(args.warmup):
         b.run()
@@ -310,7 +314,9 @@ def batched_bench(args, dev):
         "voxels": nvox,
         "batched": {"value": nvox / (batch_ms * 1e-3) / 1e9, "unit": "Gvoxel/s",
                     "ms_per_step": batch_ms, "gpu_launches": int(st["launches"]),
-                    "cuda_graph": b.uses_graph},
+                    "cuda_graph": b.uses_graph,
+                    "tuning": {k: v for k, v in tuned.items() if k != "ms"},
+                    "autotune_s": t_tune},
         "plain": {"value": nvox / (plain_ms * 1e-3) / 1e9, "unit": "Gvoxel/s",
                   "ms_per_step": plain_ms, "gpu_launches": int(plain_launches)},
         "batched_over_plain": plain_ms / batch_ms,

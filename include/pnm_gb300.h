@@ -219,6 +219,24 @@ int pnm_batch_get_stats(const pnm_batch* b, pnm_stats* out);
 /* 1 if runs replay a CUDA graph, 0 if they enqueue the stages (flag, or capture unavailable). */
 int pnm_batch_uses_graph(const pnm_batch* b);
 
+/* Launch shape of a batch's stages. Results never depend on it; the fastest shape depends on
+   the volume sizes, so pnm_batch_autotune picks it per size class. */
+typedef struct {
+  int32_t tile_z;              /* SDF-pass and flood-seed tile depth: 4, 8 or 16 (default 8) */
+  int32_t blocks_per_sm;       /* grid-stride stages: blocks of 256 threads per SM, 1..32 (8) */
+  int32_t ccl_blocks_per_sm;   /* CCL edge-union stage: blocks per SM, 1..64 (8) */
+  int32_t flood_blocks_per_sm; /* persistent flood loop: resident blocks per SM, 1..4 (2) */
+} pnm_tuning;
+#define PNM_TUNE_FORCE 1 /* time the candidates even when the cache holds the size class */
+int pnm_batch_set_tuning(pnm_batch* b, const pnm_tuning* t);
+int pnm_batch_get_tuning(const pnm_batch* b, pnm_tuning* t);
+/* Times candidate shapes on the batch's current SDFs (coordinate descent over the four knobs;
+   each candidate: one untimed and `reps` timed runs, median kept), applies the fastest and
+   records it for the (device, typical edge, volume count) class in cache_path (a text file;
+   null: no cache). A cached class is applied without timing. ms_out (optional): best run time. */
+int pnm_batch_autotune(pnm_batch* b, const char* cache_path, int32_t reps, int32_t flags,
+                       double* ms_out);
+
 /* ---- serving ----------------------------------------------------------------------------
  * No counterpart in the reference (its calls are serial and blocking, src/pnm_bindings.cpp:143).
  * A request loop over batches: every request (one periodic volume) is queued on submit and

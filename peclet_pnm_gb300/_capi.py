@@ -120,6 +120,18 @@ pnm_batch_get_stats = _sig("pnm_batch_get_stats", ctypes.c_int, _vp, _P(PnmStats
 pnm_batch_uses_graph = _sig("pnm_batch_uses_graph", ctypes.c_int, _vp)
 
 
+class PnmTuning(ctypes.Structure):
+    _fields_ = [("tile_z", _i32), ("blocks_per_sm", _i32), ("ccl_blocks_per_sm", _i32),
+                ("flood_blocks_per_sm", _i32)]
+
+
+PNM_TUNE_FORCE = 1
+pnm_batch_set_tuning = _sig("pnm_batch_set_tuning", ctypes.c_int, _vp, _P(PnmTuning))
+pnm_batch_get_tuning = _sig("pnm_batch_get_tuning", ctypes.c_int, _vp, _P(PnmTuning))
+pnm_batch_autotune = _sig("pnm_batch_autotune", ctypes.c_int, _vp, ctypes.c_char_p, _i32, _i32,
+                          _P(ctypes.c_double))
+
+
 
 class PnmServerConfig(ctypes.Structure):
     _fields_ = [("budget_bytes", _i64), ("max_inflight", _i32), ("max_batch_volumes", _i32),
@@ -161,7 +173,8 @@ EXPORTED = ["pnm_ctx_create", "pnm_ctx_destroy", "pnm_last_error", "pnm_ctx_set_
             "pnm_batch_last_error", "pnm_batch_stream", "pnm_batch_set_sdf", "pnm_batch_sdf_dev",
             "pnm_batch_launch", "pnm_batch_wait", "pnm_batch_run", "pnm_batch_volume_info",
             "pnm_batch_results_dev", "pnm_batch_copy_out", "pnm_batch_get_stats",
-            "pnm_batch_uses_graph", "pnm_server_create", "pnm_server_destroy",
+            "pnm_batch_uses_graph", "pnm_batch_set_tuning", "pnm_batch_get_tuning",
+            "pnm_batch_autotune", "pnm_server_create", "pnm_server_destroy",
             "pnm_server_last_error", "pnm_server_submit", "pnm_server_state", "pnm_server_wait",
             "pnm_server_cancel", "pnm_server_result", "pnm_server_copy_out", "pnm_server_release",
             "pnm_server_get_stats", "pnm_server_reset_stats"]

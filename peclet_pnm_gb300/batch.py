@@ -144,6 +144,27 @@ class Batch:
     def uses_graph(self) -> bool:
         return bool(_capi.pnm_batch_uses_graph(self.h))
 
+    @property
+    def tuning(self) -> dict:
+        """Launch shape of the stages (tile_z, blocks_per_sm, ccl_blocks_per_sm,
+        flood_blocks_per_sm); results never depend on it."""
+        t = _capi.PnmTuning()
+        self.check(_capi.pnm_batch_get_tuning(self.h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in _capi.PnmTuning._fields_}
+
+    def set_tuning(self, **kw):
+        t = _capi.PnmTuning(**{**self.tuning, **kw})
+        self.check(_capi.pnm_batch_set_tuning(self.h, ctypes.byref(t)))
+
+    def autotune(self, cache: str | None = None, reps: int = 3, force: bool = False) -> dict:
+        """Times candidate launch shapes on the current SDFs and keeps the fastest; `cache` (a
+        text file) remembers the choice per (device, typical edge, volume count) class."""
+        ms = ctypes.c_double()
+        self.check(_capi.pnm_batch_autotune(self.h, cache.encode() if cache else None, int(reps),
+                                            _capi.PNM_TUNE_FORCE if force else 0,
+                                            ctypes.byref(ms)))
+        return {**self.tuning, "ms": ms.value}
+
     def stats(self) -> dict:
         st = _capi.PnmStats()
         self.check(_capi.pnm_batch_get_stats(self.h, ctypes.byref(st)))

@@ -8,8 +8,11 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <new>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -49,7 +52,7 @@ long long scan_len(long long m) { return m / SCAN_TILE + 2; }
 long long rs_blocks(long long cap) { return (cap + RS_TILE - 1) / RS_TILE; }
 
 Status make_layout(int nvol, const int32_t* dims, const float* org, const float* spc,
-                   long long hash_cap, long long pore_cap, Layout* L) {
+                   long long hash_cap, long long pore_cap, Layout* L, int tile_z = 8) {
   if (nvol <= 0) return Status{PNM_ERR_ARG, "a batch needs at least one volume"};
   if (!dims) return Status{PNM_ERR_ARG, "dims is null"};
   L->vols.assign(nvol, VolDesc{});
@@ -84,7 +87,7 @@ Status make_layout(int nvol, const int32_t* dims, const float* org, const float*
     v.oy = org ? org[3 * i + 1] : 0.0f;
     v.oz = org ? org[3 * i + 2] : 0.0f;
     if (n > 0) {
-      tiles += boxes(nx, ny, nz, 32, 8, 8);
+      tiles += boxes(nx, ny, nz, 32, 8, tile_z);
       bricks += boxes(nx, ny, nz, 32, 8, 16);
     }
     L->n_total = off + n;
@@ -139,6 +142,7 @@ struct pnm_batch {
   bool own_stream = true;
   bool own_pinned = true;
   bool use_graph = true;
+  pnm_tuning tuning{8, 8, 8, 2};
   cudaGraphExec_t exec = nullptr;
   long long launches_per_run = 0;
   long long runs = 0;
@@ -208,6 +212,10 @@ Status carve(pnm_batch& b) {
   p.h_cnt = static_cast<unsigned*>(b.pinned);
   p.h_res = reinterpret_cast<pnm::VolResult*>(static_cast<char*>(b.pinned) + 256);
   p.max_sweeps = 1 << 20;
+  p.tile_z = b.tuning.tile_z;
+  p.grid_per_sm = b.tuning.blocks_per_sm;
+  p.ccl_per_sm = b.tuning.ccl_blocks_per_sm;
+  p.flood_blocks_per_sm = b.tuning.flood_blocks_per_sm;
   return Status::ok();
 }
 
@@ -227,7 +235,8 @@ Status regrow(pnm_batch& b, long long hash_cap, long long pore_cap) {
   }
   // origin / spacing stay as planned: only capacities change
   std::vector<pnm::VolDesc> keep = b.lay.vols;
-  PNM_TRY(pnm::make_layout((int)keep.size(), dims.data(), nullptr, nullptr, hash_cap, pore_cap, &L));
+  PNM_TRY(pnm::make_layout((int)keep.size(), dims.data(), nullptr, nullptr, hash_cap, pore_cap, &L,
+                           b.tuning.tile_z));
   L.vols = keep;
   PNM_CUDA(cudaStreamSynchronize(b.stream));
   drop_graph(b);
@@ -251,7 +260,7 @@ Status regrow(pnm_batch& b, long long hash_cap, long long pore_cap) {
   if (need > had) {  // a larger hash set needs larger scan partials: re-plan the arena too
     Layout full;
     PNM_TRY(pnm::make_layout((int)keep.size(), dims.data(), nullptr, nullptr, hash_cap, pore_cap,
-                             &full));
+                             &full, b.tuning.tile_z));
     const size_t sdf_bytes = (size_t)b.lay.n_total * 4;
     void* na = nullptr;
     PNM_CUDA(cudaMallocAsync(&na, full.arena, b.stream));
@@ -348,6 +357,179 @@ Status wait_checked(pnm_batch& b) {
     PNM_TRY(launch(b));
   }
   return Status{PNM_ERR_INTERNAL, "batch capacities kept growing"};
+}
+
+// ---- launch-shape tuning -------------------------------------------------------------------------
+bool tuning_valid(const pnm_tuning& t) {
+  return (t.tile_z == 4 || t.tile_z == 8 || t.tile_z == 16) && t.blocks_per_sm >= 1 &&
+         t.blocks_per_sm <= 32 && t.ccl_blocks_per_sm >= 1 && t.ccl_blocks_per_sm <= 64 &&
+         t.flood_blocks_per_sm >= 1 && t.flood_blocks_per_sm <= 4;
+}
+
+// Re-plans the tile numbering when the tile depth changes; the graph is captured again.
+Status apply_tuning(pnm_batch& b, const pnm_tuning& t) {
+  if (!tuning_valid(t)) return Status{PNM_ERR_ARG, "invalid tuning"};
+  PNM_CUDA(cudaSetDevice(b.device));
+  PNM_CUDA(cudaStreamSynchronize(b.stream));
+  if (t.tile_z != b.tuning.tile_z) {
+    long long tiles = 0;
+    for (auto& v : b.lay.vols) {
+      v.tile0 = (int)tiles;
+      if ((long long)v.nx * v.ny * v.nz > 0) tiles += pnm::boxes(v.nx, v.ny, v.nz, 32, 8, t.tile_z);
+    }
+    b.lay.tiles = tiles;
+    PNM_CUDA(cudaMemcpyAsync(const_cast<pnm::VolDesc*>(b.plan.vols), b.lay.vols.data(),
+                             b.lay.vols.size() * sizeof(pnm::VolDesc), cudaMemcpyHostToDevice,
+                             b.stream));
+    PNM_CUDA(cudaStreamSynchronize(b.stream));
+  }
+  b.tuning = t;
+  b.plan.tiles = b.lay.tiles;
+  b.plan.tile_z = t.tile_z;
+  b.plan.grid_per_sm = t.blocks_per_sm;
+  b.plan.ccl_per_sm = t.ccl_blocks_per_sm;
+  b.plan.flood_blocks_per_sm = t.flood_blocks_per_sm;
+  drop_graph(b);
+  return Status::ok();
+}
+
+// Median device time of `reps` runs enqueued without a graph (after one untimed run).
+Status time_runs(pnm_batch& b, int reps, double* ms) {
+  cudaEvent_t e0, e1;
+  PNM_CUDA(cudaEventCreate(&e0));
+  PNM_CUDA(cudaEventCreate(&e1));
+  std::vector<double> t;
+  long long nl = 0;
+  Status st = Status::ok();
+  for (int r = 0; r <= reps && st.good(); ++r) {
+    cudaEventRecord(e0, b.stream);
+    st = pnm::enqueue_batch(b.plan, b.stream, &nl);
+    cudaEventRecord(e1, b.stream);
+    if (cudaStreamSynchronize(b.stream) != cudaSuccess) st = Status{PNM_ERR_CUDA, "tuning run"};
+    float f = 0.0f;
+    cudaEventElapsedTime(&f, e0, e1);
+    if (r > 0) t.push_back(f);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  PNM_TRY(st);
+  if (b.plan.h_cnt[pnm::CNT_ERR] != 0)
+    return Status{PNM_ERR_INTERNAL, "tuning run reported a device error"};
+  std::sort(t.begin(), t.end());
+  *ms = t.empty() ? 0.0 : t[t.size() / 2];
+  return Status::ok();
+}
+
+// Size class of a batch: device, typical edge (cube root of the mean volume, in the bins the
+// batched workloads use) and the volume count's power of two.
+std::string size_class(const pnm_batch& b) {
+  cudaDeviceProp prop;
+  std::string dev = "device";
+  if (cudaGetDeviceProperties(&prop, b.device) == cudaSuccess) dev = prop.name;
+  for (char& c : dev)
+    if (c == ' ' || c == '|') c = '_';
+  const double nv = (double)b.lay.vols.size();
+  long long vox = 0;
+  for (const auto& v : b.lay.vols) vox += (long long)v.nx * v.ny * v.nz;
+  const double edge = std::cbrt((double)vox / std::max(nv, 1.0));
+  static const int bins[] = {32, 48, 64, 96, 128, 160, 192, 256, 384, 512, 768, 1024};
+  int best = bins[0];
+  for (int e : bins)
+    if (std::fabs(std::log(edge + 1.0) - std::log((double)e)) <
+        std::fabs(std::log(edge + 1.0) - std::log((double)best)))
+      best = e;
+  int nb = 0;
+  while ((1 << (nb + 1)) <= (int)nv) ++nb;
+  return dev + "|e" + std::to_string(best) + "|n" + std::to_string(1 << nb);
+}
+
+bool cache_lookup(const char* path, const std::string& key, pnm_tuning* t) {
+  if (!path) return false;
+  std::ifstream f(path);
+  std::string line;
+  bool found = false;
+  while (std::getline(f, line)) {
+    std::istringstream is(line);
+    std::string k;
+    pnm_tuning c{};
+    double ms = 0;
+    if (is >> k >> c.tile_z >> c.blocks_per_sm >> c.ccl_blocks_per_sm >> c.flood_blocks_per_sm >>
+        ms) {
+      if (k == key && tuning_valid(c)) {
+        *t = c;
+        found = true;  // the last entry wins
+      }
+    }
+  }
+  return found;
+}
+
+void cache_store(const char* path, const std::string& key, const pnm_tuning& t, double ms) {
+  if (!path) return;
+  std::vector<std::string> keep;
+  {
+    std::ifstream f(path);
+    std::string line;
+    while (std::getline(f, line)) {
+      std::istringstream is(line);
+      std::string k;
+      if ((is >> k) && k != key) keep.push_back(line);
+    }
+  }
+  const std::string tmp = std::string(path) + ".tmp";
+  {
+    std::ofstream o(tmp);
+    for (const auto& l : keep) o << l << "\n";
+    o << key << " " << t.tile_z << " " << t.blocks_per_sm << " " << t.ccl_blocks_per_sm << " "
+      << t.flood_blocks_per_sm << " " << ms << "\n";
+  }
+  std::rename(tmp.c_str(), path);
+}
+
+// Coordinate descent over the launch-shape knobs, starting from the current shape.
+Status autotune(pnm_batch& b, const char* cache, int reps, int flags, double* ms_out) {
+  if (b.lay.n_total == 0) return Status::ok();
+  const std::string key = size_class(b);
+  pnm_tuning best = b.tuning;
+  if (!(flags & PNM_TUNE_FORCE) && cache_lookup(cache, key, &best)) {
+    PNM_TRY(apply_tuning(b, best));
+    if (ms_out) *ms_out = 0.0;
+    return Status::ok();
+  }
+  // one complete run first: it grows data-dependent capacities if this data needs it
+  const bool g = b.use_graph;
+  b.use_graph = false;
+  Status st = launch(b);
+  if (st.good()) st = wait_checked(b);
+  b.use_graph = g;
+  PNM_TRY(st);
+  double best_ms = 0.0;
+  PNM_TRY(time_runs(b, reps, &best_ms));
+  const std::vector<int> tz = {4, 8, 16}, grid = {4, 8, 16}, ccl = {4, 8, 16, 32},
+                         flood = {1, 2, 4};
+  for (int knob = 0; knob < 4; ++knob) {
+    const std::vector<int>& vals = knob == 0 ? tz : knob == 1 ? ccl : knob == 2 ? grid : flood;
+    for (int v : vals) {
+      pnm_tuning c = best;
+      int* field = knob == 0 ? &c.tile_z
+                   : knob == 1 ? &c.ccl_blocks_per_sm
+                   : knob == 2 ? &c.blocks_per_sm
+                               : &c.flood_blocks_per_sm;
+      if (*field == v) continue;
+      *field = v;
+      PNM_TRY(apply_tuning(b, c));
+      double ms = 0.0;
+      PNM_TRY(time_runs(b, reps, &ms));
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = c;
+      }
+    }
+  }
+  PNM_TRY(apply_tuning(b, best));
+  cache_store(cache, key, best, best_ms);
+  if (ms_out) *ms_out = best_ms;
+  return Status::ok();
 }
 
 int fail(pnm_batch* b, Status s) {
@@ -584,5 +766,24 @@ int pnm_batch_get_stats(const pnm_batch* b, pnm_stats* out) {
 }
 
 int pnm_batch_uses_graph(const pnm_batch* b) { return b && b->exec ? 1 : 0; }
+
+int pnm_batch_set_tuning(pnm_batch* b, const pnm_tuning* t) {
+  if (!b || !t) return PNM_ERR_ARG;
+  if (b->pending) return fail(b, Status{PNM_ERR_ARG, "a run is in flight"});
+  return fail(b, apply_tuning(*b, *t));
+}
+
+int pnm_batch_get_tuning(const pnm_batch* b, pnm_tuning* t) {
+  if (!b || !t) return PNM_ERR_ARG;
+  *t = b->tuning;
+  return PNM_OK;
+}
+
+int pnm_batch_autotune(pnm_batch* b, const char* cache_path, int32_t reps, int32_t flags,
+                       double* ms_out) {
+  if (!b) return PNM_ERR_ARG;
+  if (b->pending) return fail(b, Status{PNM_ERR_ARG, "a run is in flight"});
+  return fail(b, autotune(*b, cache_path, std::max(1, (int)reps), flags, ms_out));
+}
 
 }  // extern "C"

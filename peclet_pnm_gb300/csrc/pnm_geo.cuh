@@ -176,6 +176,10 @@ struct BatchPlan {
   unsigned* h_cnt = nullptr;      // pinned mirrors, filled by the enqueued copies
   VolResult* h_res = nullptr;
   int max_sweeps = 1 << 20;
+  // launch shape (autotuned per volume-size class; results do not depend on it)
+  int tile_z = 8;               // SDF-pass / flood-seed tile depth: 4, 8 or 16
+  int grid_per_sm = 8;          // grid-stride kernels: blocks of 256 threads per SM
+  int ccl_per_sm = 8;           // CCL edge-union pass: blocks per SM
   int flood_blocks_per_sm = 2;  // persistent flood loop: resident blocks per SM
   bool pairs_in_b = false;  // set by enqueue: which radix buffer holds the sorted keys
 };

@@ -19,7 +19,8 @@
 
 namespace pnm {
 
-constexpr int TX = 32, TY = 8, TZ = 8;  // SDF-pass tile: 2048 voxels, 256 threads
+constexpr int TX = 32, TY = 8;  // SDF-pass tile: 32 x 8 x TZ voxels (TZ = 8 unless tuned), 256 threads
+constexpr int TZ_PLAIN = 8;
 constexpr int kBig = INT_MAX;           // unset min-index / non-marker parent
 
 // ---- 1. SDF pass ---------------------------------------------------------------------------
@@ -42,7 +43,7 @@ struct EdgeBuf {
 };
 constexpr int kStage = 2048;  // edges staged per block; a full stage spills straight to global
 
-template <bool ALL_ASCENT, class G>
+template <bool ALL_ASCENT, class G, int TZ = 8>
 __global__ void __launch_bounds__(TX* TY)
     k_sdf_pass(const float* __restrict__ sdf, G geo, uint8_t* __restrict__ code,
                int* __restrict__ nxt, int* __restrict__ L, uint32_t* __restrict__ peakbits,
@@ -363,7 +364,7 @@ __global__ void __launch_bounds__(256)
 // (layer 2) and from each previous layer (t >= 3). Discovery marks a layer PENDING, assignment
 // computes its labels into `tmp`, and the next discovery publishes them, so no voxel ever sees a
 // same-sweep label — exactly the double-buffered Jacobi sweep.
-template <class G>
+template <class G, int TZ = 8>
 __global__ void __launch_bounds__(TX* TY)
     k_flood_seed(G geo, const uint8_t* __restrict__ code, int* __restrict__ key, int* L,
                  int* __restrict__ ulist, unsigned* cnt) {
@@ -1020,7 +1021,7 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
   st->edge_cap = eb.cap;
   PNM_TRY(c.buf(S_NXT, n, &st->nxt));
   const OneVol geo{d, marker_threshold(spacing)};
-  const unsigned tiles = (unsigned)boxes_of(d, TX, TY, TZ);
+  const unsigned tiles = (unsigned)boxes_of(d, TX, TY, TZ_PLAIN);
   if (all_ascent)
     k_sdf_pass<true><<<tiles, TX * TY, 0, c.stream>>>(d_sdf, geo, st->code, st->nxt, L,
                                                       st->peakbits, eb, c.d_cnt);
@@ -1051,7 +1052,7 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   PNM_TRY(c.buf(S_TMP, n, &tmp));
   st->key = key;
   const unsigned vgrid = grid_for(n, 256, c.sm_count);
-  const unsigned tiles = (unsigned)boxes_of(d, TX, TY, TZ);
+  const unsigned tiles = (unsigned)boxes_of(d, TX, TY, TZ_PLAIN);
 
   k_ccl_edges<<<grid_for(n / 8 + 1, 256, c.sm_count), 256, 0, s>>>(
       st->edges, &c.d_cnt[CNT_EDGES], st->edge_cap, L, &c.d_cnt[CNT_ERR]);
@@ -1241,22 +1242,43 @@ Status enqueue_batch(BatchPlan& p, cudaStream_t s, long long* launches) {
   PNM_CUDA(cudaMemsetAsync(p.table, 0xff, p.hash_cap * sizeof(unsigned long long), s));
   k_batch_init<<<1, 1, 0, s>>>(p.range);
   const EdgeBuf eb{p.edges, p.edge_cap};
-  const unsigned vgrid = grid_for(n, 256, sm);
-  k_sdf_pass<false><<<(unsigned)p.tiles, TX * TY, 0, s>>>(p.sdf, geo, p.code, p.nxt, p.L,
-                                                          p.peakbits, eb, p.cnt);
-  k_ccl_edges<<<grid_for(n / 8 + 1, 256, sm), 256, 0, s>>>(p.edges, &p.cnt[CNT_EDGES], p.edge_cap,
-                                                           p.L, &p.cnt[CNT_ERR]);
+  const unsigned vgrid = grid_for(n, 256, sm, p.grid_per_sm);
+  const unsigned tiles = (unsigned)p.tiles;
+  switch (p.tile_z) {  // the volume table's tile numbering was planned for this depth
+    case 4:
+      k_sdf_pass<false, VolTab, 4><<<tiles, TX * TY, 0, s>>>(p.sdf, geo, p.code, p.nxt, p.L,
+                                                             p.peakbits, eb, p.cnt);
+      break;
+    case 16:
+      k_sdf_pass<false, VolTab, 16><<<tiles, TX * TY, 0, s>>>(p.sdf, geo, p.code, p.nxt, p.L,
+                                                              p.peakbits, eb, p.cnt);
+      break;
+    default:
+      k_sdf_pass<false, VolTab, 8><<<tiles, TX * TY, 0, s>>>(p.sdf, geo, p.code, p.nxt, p.L,
+                                                             p.peakbits, eb, p.cnt);
+  }
+  k_ccl_edges<<<grid_for(n / 8 + 1, 256, sm, p.ccl_per_sm), 256, 0, s>>>(
+      p.edges, &p.cnt[CNT_EDGES], p.edge_cap, p.L, &p.cnt[CNT_ERR]);
   k_ccl_all<<<vgrid, 256, 0, s>>>(geo, n, p.L, &p.cnt[CNT_EDGES], p.edge_cap, &p.cnt[CNT_ERR]);
   k_resolve<<<vgrid, 256, 0, s>>>(Dims{(int)n, 1, 1}, p.code, p.nxt, p.L, p.key, p.keylist,
                                   p.cnt);
-  k_flood_seed<<<(unsigned)p.tiles, TX * TY, 0, s>>>(geo, p.code, p.key, p.L, p.ulist, p.cnt);
+  switch (p.tile_z) {
+    case 4:
+      k_flood_seed<VolTab, 4><<<tiles, TX * TY, 0, s>>>(geo, p.code, p.key, p.L, p.ulist, p.cnt);
+      break;
+    case 16:
+      k_flood_seed<VolTab, 16><<<tiles, TX * TY, 0, s>>>(geo, p.code, p.key, p.L, p.ulist, p.cnt);
+      break;
+    default:
+      k_flood_seed<VolTab, 8><<<tiles, TX * TY, 0, s>>>(geo, p.code, p.key, p.L, p.ulist, p.cnt);
+  }
   k_flood_layer2<<<grid_for(n, 256, sm, 4), 256, 0, s>>>(
       geo, p.code, p.key, p.ulist, &p.cnt[CNT_FRONT_SPARE], p.f0, &p.cnt[CNT_FRONT0]);
   *launches += 7;
   PNM_CUDA(cudaGetLastError());
   PNM_CUDA(launch_flood_loop(geo, p.code, p.key, p.L, p.f0, p.f1, p.tmp, p.cnt, p.max_sweeps, sm,
                              n, s, p.flood_blocks_per_sm));
-  const unsigned kgrid = grid_for(n / 16 + 1, 256, sm);
+  const unsigned kgrid = grid_for(n / 16 + 1, 256, sm, p.grid_per_sm);
   k_key_first<<<kgrid, 256, 0, s>>>(p.keylist, &p.cnt[CNT_KEYS], p.L, p.code, p.firstP, p.firstS);
   exclusive_scan(PopcountOf{p.firstP}, words, p.prefP, p.scan_tmp, s, launches);
   exclusive_scan(PopcountOf{p.firstS}, words, p.prefS, p.scan_tmp, s, launches);

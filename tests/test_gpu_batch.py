@@ -114,3 +114,41 @@ def test_batch_with_empty_volumes(gpu, port):
     only_empty.run()
     assert only_empty.volume(0)["n_pores"] == 0
     only_empty.close()
+
+
+def test_launch_shapes_and_autotune_keep_results(gpu, tmp_path):
+    """Every launch shape (tile depth, grids, flood residency) gives the same bits; the autotuner
+    picks one, caches it per size class, and re-applies it from the cache."""
+    pnm, _ = gpu
+    rng = np.random.default_rng(3)
+    cases = []
+    for i in range(6):
+        shape = tuple(int(v) for v in rng.choice([20, 33, 48, 65], size=3))
+        cases.append((f"t{i}", syn.packing(shape, 0.45, mean_r=4.0, seed=300 + i)
+                      .astype(np.float32), [0, 0, 0], [1, 1, 1]))
+    cases.append(edge_cases()[0])
+    cases.append(edge_cases()[17])
+    want = [pnm.extract_pore_network(c[1], c[2], c[3], numpy=True) for c in cases]
+    b = _run(pnm, cases)
+    for shape in [dict(tile_z=4), dict(tile_z=16, blocks_per_sm=4), dict(ccl_blocks_per_sm=32),
+                  dict(tile_z=8, flood_blocks_per_sm=1, blocks_per_sm=16),
+                  dict(flood_blocks_per_sm=4, tile_z=16)]:
+        b.set_tuning(**shape)
+        b.run()
+        assert {k: b.tuning[k] for k in shape} == shape
+        for i in range(len(cases)):
+            _check(f"{shape} {i}", b.result(i), want[i])
+    cache = str(tmp_path / "tune.txt")
+    got = b.autotune(cache=cache, reps=1)
+    assert got["tile_z"] in (4, 8, 16) and got["ms"] > 0
+    assert open(cache).read().count("|e") == 1
+    b.run()
+    assert b.uses_graph
+    for i in range(len(cases)):
+        _check(f"tuned {i}", b.result(i), want[i])
+    b.close()
+    b2 = _run(pnm, cases)
+    again = b2.autotune(cache=cache)  # cached: applied without timing
+    assert again["ms"] == 0.0 and {k: again[k] for k in b2.tuning} == \
+        {k: got[k] for k in b2.tuning}
+    b2.close()
