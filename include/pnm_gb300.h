@@ -222,10 +222,10 @@ int pnm_batch_uses_graph(const pnm_batch* b);
 /* Launch shape of a batch's stages. Results never depend on it; the fastest shape depends on
    the volume sizes, so pnm_batch_autotune picks it per size class. */
 typedef struct {
-  int32_t tile_z;              /* SDF-pass and flood-seed tile depth: 4, 8 or 16 (default 8) */
-  int32_t blocks_per_sm;       /* grid-stride stages: blocks of 256 threads per SM, 1..32 (8) */
+  int32_t tile_z;              /* SDF-pass and flood-seed tile depth: 4, 8 or 16 (default 16) */
+  int32_t blocks_per_sm;       /* grid-stride stages: blocks of 256 threads per SM, 1..32 (16) */
   int32_t ccl_blocks_per_sm;   /* CCL edge-union stage: blocks per SM, 1..64 (8) */
-  int32_t flood_blocks_per_sm; /* persistent flood loop: resident blocks per SM, 1..4 (2) */
+  int32_t flood_blocks_per_sm; /* persistent flood loop: resident blocks per SM, 1..4 (4) */
 } pnm_tuning;
 #define PNM_TUNE_FORCE 1 /* time the candidates even when the cache holds the size class */
 int pnm_batch_set_tuning(pnm_batch* b, const pnm_tuning* t);

@@ -38,7 +38,7 @@ inline long long pow2_at_least(long long x) {
 struct Layout {
   std::vector<VolDesc> vols;
   long long n_total = 0, words = 0, tiles = 0, bricks = 0;
-  unsigned edge_cap = 0;
+  long long n_words = 0;  // marker-bitmap words of all volumes
   long long hash_cap = 0, pore_cap = 0;
   int label_bits = 0;
   size_t arena = 0, pairbuf = 0, porebuf = 0;
@@ -52,11 +52,11 @@ long long scan_len(long long m) { return m / SCAN_TILE + 2; }
 long long rs_blocks(long long cap) { return (cap + RS_TILE - 1) / RS_TILE; }
 
 Status make_layout(int nvol, const int32_t* dims, const float* org, const float* spc,
-                   long long hash_cap, long long pore_cap, Layout* L, int tile_z = 8) {
+                   long long hash_cap, long long pore_cap, Layout* L, int tile_z = 16) {
   if (nvol <= 0) return Status{PNM_ERR_ARG, "a batch needs at least one volume"};
   if (!dims) return Status{PNM_ERR_ARG, "dims is null"};
   L->vols.assign(nvol, VolDesc{});
-  long long off = 0, tiles = 0, bricks = 0;
+  long long off = 0, tiles = 0, bricks = 0, words = 0;
   for (int i = 0; i < nvol; ++i) {
     const int nx = dims[3 * i], ny = dims[3 * i + 1], nz = dims[3 * i + 2];
     if (nx < 0 || ny < 0 || nz < 0) return Status{PNM_ERR_ARG, "dims must be non-negative"};
@@ -70,6 +70,8 @@ Status make_layout(int nvol, const int32_t* dims, const float* org, const float*
     v.nz = nz;
     v.tile0 = (int)tiles;
     v.brick0 = (int)bricks;
+    v.word0 = (int)words;
+    words += (long long)nz * ny * ((nx + 31) / 32);
     float mn = 1.0f;
     if (spc) {
       for (int a = 0; a < 3; ++a)
@@ -97,7 +99,7 @@ Status make_layout(int nvol, const int32_t* dims, const float* org, const float*
   L->words = (n + 31) / 32;
   L->tiles = tiles;
   L->bricks = bricks;
-  L->edge_cap = (unsigned)std::min<long long>(n / 4 + 4096, (long long)UINT_MAX - 1);
+  L->n_words = std::max<long long>(words, 1);
   L->hash_cap = hash_cap > 0 ? hash_cap : pow2_at_least(std::max<long long>(1 << 14, n / 16));
   L->pore_cap = pore_cap > 0 ? pore_cap : n / 32 + 1024;
   int b = 1;
@@ -110,7 +112,7 @@ Status make_layout(int nvol, const int32_t* dims, const float* org, const float*
   a += align_up(n * 4);                     // sdf
   a += align_up(n + 64);                    // code
   a += 9 * align_up(n * 4);                 // nxt L key seg ulist keylist f0 f1 tmp
-  a += align_up((size_t)L->edge_cap * 8);   // edges
+  a += align_up((size_t)L->n_words * 4);    // marker bitmap
   a += 3 * align_up(W * 4);                 // peakbits firstP firstS
   a += 3 * align_up((W + 1) * 4);           // prefP prefS peakpref
   a += align_up(sl * 4);                    // scan partials
@@ -142,7 +144,7 @@ struct pnm_batch {
   bool own_stream = true;
   bool own_pinned = true;
   bool use_graph = true;
-  pnm_tuning tuning{8, 8, 8, 2};
+  pnm_tuning tuning{16, 16, 8, 4};
   cudaGraphExec_t exec = nullptr;
   long long launches_per_run = 0;
   long long runs = 0;
@@ -177,8 +179,8 @@ Status carve(pnm_batch& b) {
   p.code = reinterpret_cast<uint8_t*>(take(n + 64));
   int** ints[] = {&p.nxt, &p.L, &p.key, &p.seg, &p.ulist, &p.keylist, &p.f0, &p.f1, &p.tmp};
   for (int** q : ints) *q = reinterpret_cast<int*>(take(n * 4));
-  p.edge_cap = L.edge_cap;
-  p.edges = reinterpret_cast<int2*>(take((size_t)L.edge_cap * 8));
+  p.n_words = L.n_words;
+  p.mbits = reinterpret_cast<uint32_t*>(take((size_t)L.n_words * 4));
   p.peakbits = reinterpret_cast<uint32_t*>(take(W * 4));
   p.firstP = reinterpret_cast<uint32_t*>(take(W * 4));
   p.firstS = reinterpret_cast<uint32_t*>(take(W * 4));

@@ -49,7 +49,7 @@ enum Counter : int {
   CNT_FRONT0,        // flood frontier length, ping
   CNT_FRONT1,        // flood frontier length, pong
   CNT_FRONT_SPARE,   // flood voxels without a marker neighbour (list U)
-  CNT_EDGES,         // marker-CCL edges emitted by the SDF pass
+  CNT_EDGES,         // marker-CCL links united (run pairs that touch)
   CNT_FLOW_SPARE0,
   CNT_FLOW_SPARE1,
   CNT_SWEEPS,        // flood sweeps run by the persistent flood loop
@@ -129,9 +129,9 @@ struct SegState {
   int32_t* key = nullptr;       // per voxel: basin root (>=0), ~solid label (<0), INT_MIN none
   int32_t* idtab = nullptr;     // per key voxel: final signed label id
   uint32_t* peakbits = nullptr; // bitmap of extract_pores peaks
-  int2* edges = nullptr;        // marker-CCL edges (run head, neighbouring run representative)
-  unsigned edge_cap = 0;
-  unsigned n_edges = 0;
+  uint32_t* mbits = nullptr;    // marker bitmap, one word per 32-voxel row chunk
+  long long n_words = 0;
+  unsigned n_edges = 0;         // marker-CCL links united
   int n_pore_labels = 0;        // np
   int n_solid_labels = 0;
   int flood_sweeps = 0;

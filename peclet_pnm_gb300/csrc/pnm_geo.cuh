@@ -23,8 +23,9 @@ namespace pnm {
 struct VolDesc {
   int off;            // first global voxel id (multiple of 32)
   int nx, ny, nz;
-  int tile0;          // first SDF-pass tile (32 x 8 x 8) of this volume, batch-wide numbering
-  int brick0;         // first seg/topology brick (32 x 8 x 16)
+  int tile0;          // first SDF-pass tile (32 x 8 x tile depth) of this volume, batch-wide
+  int brick0;         // first resolve / seg-topology brick (32 x 8 x 16)
+  int word0;          // first marker-bitmap word (one per 32-voxel row chunk)
   float thr;          // marker threshold: -1.5 * min spacing (pore_extraction.hpp:163-164)
   float ox, oy, oz;   // origin, xyz
   float sx, sy, sz;   // spacing, xyz
@@ -44,6 +45,7 @@ struct VolResult {
 // One tile (or brick) of one volume: what a block of a tiled kernel works on.
 struct Box {
   int off, nx, ny, nz;
+  int word0;
   int X0, Y0, Z0;
   int vol;
   float thr;
@@ -67,6 +69,7 @@ struct OneVol {
   __device__ Box tile(int b, int TXv, int TYv, int TZv, bool /*brick*/) const {
     Box x;
     x.off = 0;
+    x.word0 = 0;
     x.nx = d.nx;
     x.ny = d.ny;
     x.nz = d.nz;
@@ -84,6 +87,13 @@ struct OneVol {
   }
   __device__ int vol_of(int /*v*/) const { return 0; }
   __device__ int gbase(int /*vol*/) const { return 0; }
+  __device__ void locate_word(int /*w*/, int& off, int& nx, int& ny, int& nz, int& word0) const {
+    off = 0;
+    word0 = 0;
+    nx = d.nx;
+    ny = d.ny;
+    nz = d.nz;
+  }
 };
 
 // A ragged batch: binary searches over the volume table (a few dozen to a few thousand entries,
@@ -116,6 +126,7 @@ struct VolTab {
     const int i = find_tile(b, brick);
     Box x;
     x.off = __ldg(&v[i].off);
+    x.word0 = __ldg(&v[i].word0);
     x.nx = __ldg(&v[i].nx);
     x.ny = __ldg(&v[i].ny);
     x.nz = __ldg(&v[i].nz);
@@ -132,6 +143,19 @@ struct VolTab {
     nz = __ldg(&v[i].nz);
   }
   __device__ int gbase(int vol) const { return r[vol].gbase; }
+  __device__ void locate_word(int w, int& off, int& nx, int& ny, int& nz, int& word0) const {
+    int lo = 0, hi = nvol - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(&v[mid].word0) <= w) lo = mid;
+      else hi = mid - 1;
+    }
+    off = __ldg(&v[lo].off);
+    word0 = __ldg(&v[lo].word0);
+    nx = __ldg(&v[lo].nx);
+    ny = __ldg(&v[lo].ny);
+    nz = __ldg(&v[lo].nz);
+  }
   // volume owning batch-wide pair label g
   __device__ int vol_of_label(int g) const {
     int lo = 0, hi = nvol - 1;
@@ -158,8 +182,8 @@ struct BatchPlan {
   uint8_t* code = nullptr;
   int *nxt = nullptr, *L = nullptr, *key = nullptr, *seg = nullptr;
   int *ulist = nullptr, *keylist = nullptr, *f0 = nullptr, *f1 = nullptr, *tmp = nullptr;
-  int2* edges = nullptr;
-  unsigned edge_cap = 0;
+  uint32_t* mbits = nullptr;  // marker bitmap: one word per 32-voxel row chunk of every volume
+  long long n_words = 0;
   uint32_t *peakbits = nullptr, *firstP = nullptr, *firstS = nullptr;
   unsigned *prefP = nullptr, *prefS = nullptr, *peakpref = nullptr, *scan_tmp = nullptr;
   unsigned long long* table = nullptr;
@@ -177,10 +201,10 @@ struct BatchPlan {
   VolResult* h_res = nullptr;
   int max_sweeps = 1 << 20;
   // launch shape (autotuned per volume-size class; results do not depend on it)
-  int tile_z = 8;               // SDF-pass / flood-seed tile depth: 4, 8 or 16
-  int grid_per_sm = 8;          // grid-stride kernels: blocks of 256 threads per SM
+  int tile_z = 16;              // SDF-pass / flood-seed tile depth: 4, 8 or 16
+  int grid_per_sm = 16;         // grid-stride kernels: blocks of 256 threads per SM
   int ccl_per_sm = 8;           // CCL edge-union pass: blocks per SM
-  int flood_blocks_per_sm = 2;  // persistent flood loop: resident blocks per SM
+  int flood_blocks_per_sm = 4;  // persistent flood loop: resident blocks per SM
   bool pairs_in_b = false;  // set by enqueue: which radix buffer holds the sorted keys
 };
 

@@ -20,7 +20,10 @@
 namespace pnm {
 
 constexpr int TX = 32, TY = 8;  // SDF-pass tile: 32 x 8 x TZ voxels (TZ = 8 unless tuned), 256 threads
-constexpr int TZ_PLAIN = 8;
+// launch shape of the single-volume entry points (the batch path tunes its own)
+constexpr int TZ_PLAIN = 16;           // SDF-pass / flood-seed tile depth
+constexpr int PLAIN_GRID_PER_SM = 16;  // grid-stride stages: blocks per SM
+constexpr int PLAIN_FLOOD_PER_SM = 4;  // persistent flood loop: resident blocks per SM
 constexpr int kBig = INT_MAX;           // unset min-index / non-marker parent
 
 // ---- 1. SDF pass ---------------------------------------------------------------------------
@@ -33,28 +36,19 @@ constexpr int kBig = INT_MAX;           // unset min-index / non-marker parent
 //  * class (marker :177, flood :245-248, pore :276), flood seed (has a marker neighbour), peak
 //    bit for extract_pores (:89-106): !(sdf <= 0) and the voxel is its own ascent target.
 // Marker CCL (:181-230), first half: a marker's union-find parent is the first marker of its run
-// inside the chunk (runs are connected). Adjacency to the 13 forward neighbours (:204-206) is
-// emitted as edges (run head, head of a touching run of the four forward rows, or the voxel
-// across the chunk end); lanes drop links the previous lane already made, each warp reserves
-// its edges with one shared-memory atomic and each block with one global atomic.
-struct EdgeBuf {
-  int2* e;
-  unsigned cap;
-};
-constexpr int kStage = 2048;  // edges staged per block; a full stage spills straight to global
+// inside the 32-voxel chunk (runs are connected), and the chunk's marker bits go to the marker
+// bitmap (one word per chunk, bits past the volume's x extent clear) for k_ccl_words.
 
 template <bool ALL_ASCENT, class G, int TZ = 8>
 __global__ void __launch_bounds__(TX* TY)
     k_sdf_pass(const float* __restrict__ sdf, G geo, uint8_t* __restrict__ code,
                int* __restrict__ nxt, int* __restrict__ L, uint32_t* __restrict__ peakbits,
-               EdgeBuf eb, unsigned* cnt) {
+               uint32_t* __restrict__ mbits) {
   constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2, NT = TX * TY;
   __shared__ float s[HZ][HY][HX];
   __shared__ int wx[HX], wy[HY], wz[HZ];
   __shared__ unsigned rowm[HZ][HY];       // markers of each halo row at x = X0 .. X0+31
   __shared__ unsigned char rowh[HZ][HY];  // bit 0: marker at x = X0-1; bit 1: at x = X0+32
-  __shared__ int2 stage[kStage];
-  __shared__ unsigned nstage, gbase;
   const Box bx = geo.tile(blockIdx.x, TX, TY, TZ, false);
   const int off = bx.off;  // the volume's first global voxel id: added to every stored id
   const float thr = bx.thr;
@@ -68,7 +62,6 @@ __global__ void __launch_bounds__(TX* TY)
   const int X0 = bx.X0, Y0 = bx.Y0, Z0 = bx.Z0;
   const int t = threadIdx.x;
   const int lane = t & 31;  // == tx (TX == 32)
-  if (t == 0) nstage = 0;
   if (G::kBatch && bx.first) {  // the gap up to the next volume: never-labelled ZERO codes
     const int n = nx * ny * nz;
     for (int i = n + t; i < ((n + 31) & ~31); i += NT) code[i] = make_code(kSelf, CLS_ZERO, false);
@@ -168,168 +161,172 @@ __global__ void __launch_bounds__(TX* TY)
     const int hl = marker ? 31 - __clz((m & ~(m << 1)) & upto) : 0;
     const int head = off + gz * nxy + gy * nx + X0 + hl;
     if (valid) L[ci] = marker ? head : kBig;
-    if (!__any_sync(0xffffffffu, marker)) continue;
-    // links: up to two touching runs per forward row plus the +x voxel across the chunk end
-    int rep[9];
-    unsigned have = 0;
-#pragma unroll
-    for (int f = 0; f < 4; ++f) {  // forward rows (dy,dz) = (1,0), (-1,1), (0,1), (1,1)
-      const int sy = ty + 1 + ((f == 0 || f == 3) ? 1 : (f == 1 ? -1 : 0));
-      const int sz = tz + 1 + (f == 0 ? 0 : 1);
-      const unsigned m2 = rowm[sz][sy];
-      const unsigned hb = rowh[sz][sy];
-      const unsigned st2 = m2 & ~(m2 << 1);
-      int c0 = -2, c1 = -2;  // chunk positions; -1 / 32: the halo columns
-      if (marker) {
-        if ((m2 >> lane) & 1u) {
-          c0 = 31 - __clz(st2 & upto);
-        } else {
-          if (lane > 0) {
-            if ((m2 >> (lane - 1)) & 1u) c0 = 31 - __clz(st2 & (upto >> 1));
-          } else if (hb & 1u) {
-            c0 = -1;
-          }
-          if (lane < 31) {
-            if ((m2 >> (lane + 1)) & 1u) c1 = lane + 1;
-          } else if (hb & 2u) {
-            c1 = 32;
-          }
-        }
-      }
-      const int p0 = __shfl_up_sync(0xffffffffu, c0, 1);
-      const int p1 = __shfl_up_sync(0xffffffffu, c1, 1);
-      const int ph = __shfl_up_sync(0xffffffffu, head, 1);
-      const bool same = lane > 0 && ph == head;
-      const int rowg = wz[sz] * nxy + wy[sy] * nx;
-      if (c0 != -2 && !(same && (c0 == p0 || c0 == p1))) {
-        rep[2 * f] = rowg + wx[c0 + 1];
-        have |= 1u << (2 * f);
-      }
-      if (c1 != -2 && !(same && (c1 == p0 || c1 == p1))) {
-        rep[2 * f + 1] = rowg + wx[c1 + 1];
-        have |= 1u << (2 * f + 1);
-      }
-    }
-    if (marker && (lane == 31 || gx + 1 == nx) && s[tz + 1][ty + 1][tx + 2] < thr) {
-      rep[8] = gz * nxy + gy * nx + wx[tx + 2];
-      have |= 1u << 8;
-    }
-    // warp-compacted staging: one shared-memory reservation per warp
-    const unsigned mine = __popc(have);
-    unsigned incl = mine;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
-    unsigned base = 0;
-    if (lane == 0 && total) base = atomicAdd(&nstage, total);
-    base = __shfl_sync(0xffffffffu, base, 0) + incl - mine;
-#pragma unroll
-    for (int j = 0; j < 9; ++j) {
-      if (!((have >> j) & 1u)) continue;
-      const int2 e = make_int2(head, off + rep[j]);
-      if (base < (unsigned)kStage) {
-        stage[base] = e;
-      } else {
-        const unsigned g = atomicAdd(&cnt[CNT_EDGES], 1u);
-        if (g < eb.cap) eb.e[g] = e;
-      }
-      ++base;
+    if (lane == 0 && gy < ny && gz < nz) {
+      const int xe = nx - X0;  // valid x positions of this chunk
+      mbits[bx.word0 + (gz * ny + gy) * ((nx + 31) >> 5) + (X0 >> 5)] =
+          m & (xe >= 32 ? 0xffffffffu : ((1u << xe) - 1u));
     }
   }
-  __syncthreads();
-  const unsigned ns = min(nstage, (unsigned)kStage);
-  if (t == 0) gbase = ns ? atomicAdd(&cnt[CNT_EDGES], ns) : 0u;
-  __syncthreads();
-  for (unsigned i = t; i < ns; i += NT)
-    if (gbase + i < eb.cap) eb.e[gbase + i] = stage[i];
 }
 
 // ---- 2. marker CCL, second half ------------------------------------------------------------
-// Unites the emitted edges. The surviving root of a component is its minimum voxel id, the
-// reference's canonical label (pore_extraction.hpp:217-219).
-__global__ void __launch_bounds__(256) k_ccl_edges(const int2* __restrict__ e, const unsigned* n_p,
-                                                   unsigned cap, int* L, unsigned* err) {
-  const unsigned n = min(*n_p, cap);
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int2 ab = e[i];
-    uf_unite(L, ab.x, ab.y, err);
-  }
-}
-
-// Fallback when the edge buffer overflowed (adversarial marker patterns): every marker unites
-// with its 13 forward periodic neighbours directly; lanes proposing the same (parent, parent)
-// link issue one union. Launched unconditionally inside a captured batch: it returns at once
-// unless the edge count exceeded the buffer.
+// One thread per marker-bitmap word (a 32-voxel row chunk). For every run of the word (a
+// union-find node, identified by its first voxel) it unites the nodes its 13 forward neighbours
+// (pore_extraction.hpp:204-206) touch: the next node along +x (across the chunk end, or the
+// periodic wrap at the volume end), and in each forward row (dy,dz) = (1,0), (-1,1), (0,1), (1,1)
+// the node covering x_start-1 and every node starting in [x_start, x_end+1] (positions wrap).
+// Links go straight into the union-find (link to the smaller root), so the surviving root of a
+// component is its minimum voxel id, the reference's canonical label (:217-219).
 template <class G>
 __global__ void __launch_bounds__(256)
-    k_ccl_all(G geo, long long n, int* L, const unsigned* n_edges_p, unsigned cap, unsigned* err) {
-  if (n_edges_p && *n_edges_p <= cap) return;
-  for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
-       base += (long long)gridDim.x * blockDim.x) {
-    const long long vl = base + threadIdx.x;
-    const int v = (int)vl;
-    int off = 0, nx = 1, ny = 1, nz = 1;
-    if (vl < n) geo.locate(v, off, nx, ny, nz);
-    const int lv = v - off;
-    const bool inside = vl < n && lv < nx * ny * nz;  // not in the gap after a volume
-    const int a = inside ? ld_relaxed(&L[v]) : kBig;
-    const int x = lv % nx, y = (lv / nx) % ny, z = lv / (nx * ny);
-#pragma unroll 1
-    for (int k = 0; k < 13; ++k) {
-      const int dz = k < 9 ? 1 : 0;
-      const int dy = k < 9 ? (k / 3) - 1 : (k < 12 ? 1 : 0);
-      const int dx = k < 12 ? (k % 3) - 1 : 1;
-      unsigned long long pk = ~0ull;
-      int b = kBig;
-      if (a != kBig) {
-        b = ld_relaxed(&L[off + (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx +
-                          wrap1(x + dx, nx)]);
-        if (b != kBig && b != a) pk = ((unsigned long long)(unsigned)a << 32) | (unsigned)b;
+    k_ccl_words(G geo, const uint32_t* __restrict__ mbits, long long n_words, int* L,
+                unsigned* cnt) {
+  unsigned* err = &cnt[CNT_ERR];
+  unsigned links = 0;
+  for (long long wi = (long long)blockIdx.x * blockDim.x + threadIdx.x; wi < n_words;
+       wi += (long long)gridDim.x * blockDim.x) {
+    const uint32_t m = __ldg(&mbits[wi]);
+    if (!m) continue;
+    int off, nx, ny, nz, word0;
+    geo.locate_word((int)wi, off, nx, ny, nz, word0);
+    const int ncx = (nx + 31) >> 5;
+    const int lw = (int)wi - word0;
+    const int c = lw % ncx, row = lw / ncx;
+    const int y = row % ny, z = row / ny;
+    const uint32_t* vb = mbits + word0;
+    // node (first voxel of the chunk-local run) covering x of row (z2, y2), or -1
+    auto node_at = [&](int z2, int y2, int x) -> int {
+      const int c2 = x >> 5, b = x & 31;
+      const uint32_t w = __ldg(&vb[(z2 * ny + y2) * ncx + c2]);
+      if (!((w >> b) & 1u)) return -1;
+      const uint32_t st = w & ~(w << 1);
+      return off + (z2 * ny + y2) * nx + (c2 << 5) + 31 - __clz(st & ((2u << b) - 1u));
+    };
+    uint32_t rem = m;
+    while (rem) {
+      const int p = __ffs(rem) - 1;
+      const int len = __ffsll(~(unsigned long long)(rem >> p)) - 1;
+      rem &= len == 32 ? 0u : ~(((1u << len) - 1u) << p);
+      const int e = p + len - 1;
+      const int xs = (c << 5) + p, xe = (c << 5) + e;
+      const int head = off + (z * ny + y) * nx + xs;
+      // +x: the node after the run in this row
+      {
+        int t = -1;
+        if (xe == nx - 1) t = node_at(z, y, 0);
+        else if (e == 31 && (__ldg(&vb[(z * ny + y) * ncx + c + 1]) & 1u))
+          t = off + (z * ny + y) * nx + ((c + 1) << 5);
+        if (t >= 0) {
+          uf_unite(L, head, t, err);
+          ++links;
+        }
       }
-      const unsigned peers = __match_any_sync(0xffffffffu, pk);
-      if (pk != ~0ull && (__ffs(peers) - 1) == (int)lane_id()) uf_unite(L, a, b, err);
+#pragma unroll
+      for (int f = 0; f < 4; ++f) {
+        const int dy = (f == 0 || f == 3) ? 1 : (f == 1 ? -1 : 0), dz = f == 0 ? 0 : 1;
+        const int y2 = wrap1(y + dy, ny), z2 = wrap1(z + dz, nz);
+        const int rowb = off + (z2 * ny + y2) * nx;
+        int t = node_at(z2, y2, xs == 0 ? nx - 1 : xs - 1);
+        if (t >= 0) {
+          uf_unite(L, head, t, err);
+          ++links;
+        }
+        const uint32_t w2 = __ldg(&vb[(z2 * ny + y2) * ncx + c]);
+        const int hi = e + 1 > 31 ? 31 : e + 1;
+        uint32_t sm = (w2 & ~(w2 << 1)) & ((2u << hi) - 1u) & ~((1u << p) - 1u);
+        while (sm) {
+          const int b = __ffs(sm) - 1;
+          sm &= sm - 1;
+          uf_unite(L, head, rowb + (c << 5) + b, err);
+          ++links;
+        }
+        t = -1;
+        if (xe + 1 == nx) t = node_at(z2, y2, 0);
+        else if (e == 31 && (__ldg(&vb[(z2 * ny + y2) * ncx + c + 1]) & 1u))
+          t = rowb + ((c + 1) << 5);
+        if (t >= 0) {
+          uf_unite(L, head, t, err);
+          ++links;
+        }
+      }
     }
   }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) links += __shfl_xor_sync(0xffffffffu, links, o);
+  if ((threadIdx.x & 31) == 0 && links) atomicAdd(&cnt[CNT_EDGES], links);
 }
 
 // ---- 3. resolve ----------------------------------------------------------------------------------
-// Gradient root of a voxel: follow the ascent pointers for at most 512 moves
-// (pore_extraction.hpp:277-309 and :626-648; MAX_STEPS = 512).
-
+// Gradient root of a voxel: follow the ascent for at most 512 moves (pore_extraction.hpp:277-309
+// and :626-648; MAX_STEPS = 512). The kernel works on 32 x 8 x 16 bricks whose code bytes sit in
+// shared memory: a walk follows the direction bits there while it stays inside the brick (one
+// move per step, no global load), and continues with the global ascent pointers once it leaves
+// the brick (or would wrap), counting every move, so the cap is exact.
+constexpr int RTX = 32, RTY = 8, RTZ = 16;
 
 // For every voxel: marker -> key ~root(CCL), the root joins the key list; pore -> key = gradient
 // root, atomicMin of the voxel id into L[root] (its first-appearance index; pore voxels' L started
 // at kBig) and, on first touch, the root joins the key list; flood and zero voxels -> KEY_NONE
-// (flood labels follow in k_flood_seed). Lanes of a warp whose markers share a union-find parent
-// run one find for the group.
-__global__ void __launch_bounds__(256)
-    k_resolve(Dims d, const uint8_t* __restrict__ code, const int* __restrict__ nxt, int* L,
+// (flood labels follow in k_flood_seed). Lanes of a warp hold consecutive voxels of a row; lanes
+// whose markers share a union-find parent run one find for the group.
+template <class G>
+__global__ void __launch_bounds__(RTX* RTY)
+    k_resolve(G geo, const uint8_t* __restrict__ code, const int* __restrict__ nxt, int* L,
               int* __restrict__ key, int* __restrict__ keylist, unsigned* cnt) {
-  const long long n = d.n();
+  __shared__ uint8_t cb[RTZ][RTY][RTX];
   unsigned* err = &cnt[CNT_ERR];
-  for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
-       base += (long long)gridDim.x * blockDim.x) {
-    const long long vl = base + threadIdx.x;
-    const bool valid = vl < n;
-    const int v = (int)vl;
+  const Box bx = geo.tile(blockIdx.x, RTX, RTY, RTZ, true);
+  const int off = bx.off, nx = bx.nx, ny = bx.ny, nz = bx.nz;
+  const int nxy = nx * ny;
+  const int X0 = bx.X0, Y0 = bx.Y0, Z0 = bx.Z0;
+  const int TXe = min(RTX, nx - X0), TYe = min(RTY, ny - Y0), TZe = min(RTZ, nz - Z0);
+  const int lane = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < RTX * RTY * RTZ; i += RTX * RTY) {
+    const int lx = i % RTX, ly = (i / RTX) % RTY, lz = i / (RTX * RTY);
+    cb[lz][ly][lx] = (lx < TXe && ly < TYe && lz < TZe)
+                         ? __ldg(&code[off + (Z0 + lz) * nxy + (Y0 + ly) * nx + X0 + lx])
+                         : make_code(kSelf, CLS_ZERO, false);
+  }
+  __syncthreads();
+  const bool inxy = lane < TXe && ty < TYe;
+  for (int tz = 0; tz < RTZ; ++tz) {
+    const bool valid = inxy && tz < TZe;
+    const int v = off + (Z0 + tz) * nxy + (Y0 + ty) * nx + X0 + lane;
     int k = KEY_NONE, agg = -1, par = -1;
     bool new_key = false;
     if (valid) {
-      const uint8_t c = code[v];
+      const uint8_t c = cb[tz][ty][lane];
       const int cls = code_cls(c);
       if (cls == CLS_MARKER) {
         par = ld_relaxed(&L[v]);
       } else if (cls == CLS_PORE) {
-        const int r = chase_root(nxt, v);
-        k = r;
-        agg = r;
+        int x = lane, y = ty, z = tz, moves = 0;
+        bool root = false;
+        while (moves < 512) {  // inside the brick: direction bits
+          const int dk = code_dir(cb[z][y][x]);
+          if (dk == kSelf) {
+            root = true;
+            break;
+          }
+          const int x2 = x + dk % 3 - 1, y2 = y + (dk / 3) % 3 - 1, z2 = z + dk / 9 - 1;
+          if (x2 < 0 || x2 >= TXe || y2 < 0 || y2 >= TYe || z2 < 0 || z2 >= TZe) break;
+          x = x2;
+          y = y2;
+          z = z2;
+          ++moves;
+        }
+        int cur = off + (Z0 + z) * nxy + (Y0 + y) * nx + X0 + x;
+        if (!root) {  // left the brick: the global pointers for the remaining moves
+          for (; moves < 512; ++moves) {
+            const int n2 = __ldg(&nxt[cur]);
+            if (n2 == cur) break;
+            cur = n2;
+          }
+        }
+        k = cur;
+        agg = cur;
       }
     }
-    const unsigned lane = lane_id();
     {  // one find per run of lanes sharing a parent (lanes hold consecutive voxels)
       const int pp = __shfl_up_sync(0xffffffffu, par, 1);
       const bool lead = par >= 0 && (lane == 0 || pp != par);
@@ -1005,7 +1002,6 @@ cudaError_t launch_flood_loop(G geo, const uint8_t* code, int* key, int* L, int*
 Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st,
                     bool all_ascent) {
   const long long n = d.n();
-  PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_EDGES], 0, sizeof(unsigned), c.stream));
   const long long words = (n + 31) / 32;
   st->d = d;
   st->sdf = d_sdf;
@@ -1014,20 +1010,17 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
   PNM_TRY(c.buf(S_L, n, &L));
   PNM_TRY(c.buf(S_PEAKBITS, words, &st->peakbits));
   PNM_CUDA(cudaMemsetAsync(st->peakbits, 0, words * sizeof(uint32_t), c.stream));
-  EdgeBuf eb;
-  eb.cap = (unsigned)std::min<long long>(n / 4 + 4096, (long long)UINT_MAX - 1);
-  PNM_TRY(c.buf(S_EDGES, eb.cap, &eb.e));
-  st->edges = eb.e;
-  st->edge_cap = eb.cap;
+  st->n_words = (long long)d.nz * d.ny * ((d.nx + 31) / 32);
+  PNM_TRY(c.buf(S_EDGES, st->n_words, &st->mbits));
   PNM_TRY(c.buf(S_NXT, n, &st->nxt));
   const OneVol geo{d, marker_threshold(spacing)};
   const unsigned tiles = (unsigned)boxes_of(d, TX, TY, TZ_PLAIN);
   if (all_ascent)
-    k_sdf_pass<true><<<tiles, TX * TY, 0, c.stream>>>(d_sdf, geo, st->code, st->nxt, L,
-                                                      st->peakbits, eb, c.d_cnt);
+    k_sdf_pass<true, OneVol, TZ_PLAIN><<<tiles, TX * TY, 0, c.stream>>>(
+        d_sdf, geo, st->code, st->nxt, L, st->peakbits, st->mbits);
   else
-    k_sdf_pass<false><<<tiles, TX * TY, 0, c.stream>>>(d_sdf, geo, st->code, st->nxt, L,
-                                                       st->peakbits, eb, c.d_cnt);
+    k_sdf_pass<false, OneVol, TZ_PLAIN><<<tiles, TX * TY, 0, c.stream>>>(
+        d_sdf, geo, st->code, st->nxt, L, st->peakbits, st->mbits);
   ++c.launches;
   PNM_CUDA(cudaGetLastError());
   st->idtab = L;
@@ -1051,16 +1044,13 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   PNM_TRY(c.buf(S_FRONT1, n, &f1));
   PNM_TRY(c.buf(S_TMP, n, &tmp));
   st->key = key;
-  const unsigned vgrid = grid_for(n, 256, c.sm_count);
   const unsigned tiles = (unsigned)boxes_of(d, TX, TY, TZ_PLAIN);
 
-  k_ccl_edges<<<grid_for(n / 8 + 1, 256, c.sm_count), 256, 0, s>>>(
-      st->edges, &c.d_cnt[CNT_EDGES], st->edge_cap, L, &c.d_cnt[CNT_ERR]);
-  // overflow fallback: returns at once unless the edge buffer overflowed
-  k_ccl_all<<<vgrid, 256, 0, s>>>(geo, n, L, &c.d_cnt[CNT_EDGES], st->edge_cap,
-                                  &c.d_cnt[CNT_ERR]);
-  k_resolve<<<vgrid, 256, 0, s>>>(d, st->code, st->nxt, L, key, keylist, c.d_cnt);
-  k_flood_seed<<<tiles, TX * TY, 0, s>>>(geo, st->code, key, L, ulist, c.d_cnt);
+  k_ccl_words<<<grid_for(st->n_words, 256, c.sm_count, PLAIN_GRID_PER_SM), 256, 0, s>>>(
+      geo, st->mbits, st->n_words, L, c.d_cnt);
+  k_resolve<<<(unsigned)boxes_of(d, RTX, RTY, RTZ), RTX * RTY, 0, s>>>(geo, st->code, st->nxt, L,
+                                                                      key, keylist, c.d_cnt);
+  k_flood_seed<OneVol, TZ_PLAIN><<<tiles, TX * TY, 0, s>>>(geo, st->code, key, L, ulist, c.d_cnt);
   const unsigned fgrid = grid_for(n, 256, c.sm_count, 4);
   k_flood_layer2<<<fgrid, 256, 0, s>>>(geo, st->code, key, ulist, &c.d_cnt[CNT_FRONT_SPARE], f0,
                                        &c.d_cnt[CNT_FRONT0]);
@@ -1071,7 +1061,7 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   // separate launches in batches between host checks (empty sweeps are no-ops)
   const int kMaxSweeps = 1 << 20;
   cudaError_t le = launch_flood_loop(geo, st->code, key, L, f0, f1, tmp, c.d_cnt, kMaxSweeps,
-                                     c.sm_count, n, s);
+                                     c.sm_count, n, s, PLAIN_FLOOD_PER_SM);
   ++c.launches;
   if (le != cudaSuccess) {
     cudaGetLastError();
@@ -1241,27 +1231,24 @@ Status enqueue_batch(BatchPlan& p, cudaStream_t s, long long* launches) {
   PNM_CUDA(cudaMemsetAsync(p.firstS, 0, words * sizeof(uint32_t), s));
   PNM_CUDA(cudaMemsetAsync(p.table, 0xff, p.hash_cap * sizeof(unsigned long long), s));
   k_batch_init<<<1, 1, 0, s>>>(p.range);
-  const EdgeBuf eb{p.edges, p.edge_cap};
-  const unsigned vgrid = grid_for(n, 256, sm, p.grid_per_sm);
   const unsigned tiles = (unsigned)p.tiles;
   switch (p.tile_z) {  // the volume table's tile numbering was planned for this depth
     case 4:
       k_sdf_pass<false, VolTab, 4><<<tiles, TX * TY, 0, s>>>(p.sdf, geo, p.code, p.nxt, p.L,
-                                                             p.peakbits, eb, p.cnt);
+                                                             p.peakbits, p.mbits);
       break;
     case 16:
       k_sdf_pass<false, VolTab, 16><<<tiles, TX * TY, 0, s>>>(p.sdf, geo, p.code, p.nxt, p.L,
-                                                              p.peakbits, eb, p.cnt);
+                                                             p.peakbits, p.mbits);
       break;
     default:
       k_sdf_pass<false, VolTab, 8><<<tiles, TX * TY, 0, s>>>(p.sdf, geo, p.code, p.nxt, p.L,
-                                                             p.peakbits, eb, p.cnt);
+                                                             p.peakbits, p.mbits);
   }
-  k_ccl_edges<<<grid_for(n / 8 + 1, 256, sm, p.ccl_per_sm), 256, 0, s>>>(
-      p.edges, &p.cnt[CNT_EDGES], p.edge_cap, p.L, &p.cnt[CNT_ERR]);
-  k_ccl_all<<<vgrid, 256, 0, s>>>(geo, n, p.L, &p.cnt[CNT_EDGES], p.edge_cap, &p.cnt[CNT_ERR]);
-  k_resolve<<<vgrid, 256, 0, s>>>(Dims{(int)n, 1, 1}, p.code, p.nxt, p.L, p.key, p.keylist,
-                                  p.cnt);
+  k_ccl_words<<<grid_for(p.n_words, 256, sm, p.ccl_per_sm), 256, 0, s>>>(geo, p.mbits, p.n_words,
+                                                                          p.L, p.cnt);
+  k_resolve<<<(unsigned)p.bricks, RTX * RTY, 0, s>>>(geo, p.code, p.nxt, p.L, p.key, p.keylist,
+                                                     p.cnt);
   switch (p.tile_z) {
     case 4:
       k_flood_seed<VolTab, 4><<<tiles, TX * TY, 0, s>>>(geo, p.code, p.key, p.L, p.ulist, p.cnt);
@@ -1274,7 +1261,7 @@ Status enqueue_batch(BatchPlan& p, cudaStream_t s, long long* launches) {
   }
   k_flood_layer2<<<grid_for(n, 256, sm, 4), 256, 0, s>>>(
       geo, p.code, p.key, p.ulist, &p.cnt[CNT_FRONT_SPARE], p.f0, &p.cnt[CNT_FRONT0]);
-  *launches += 7;
+  *launches += 6;
   PNM_CUDA(cudaGetLastError());
   PNM_CUDA(launch_flood_loop(geo, p.code, p.key, p.L, p.f0, p.f1, p.tmp, p.cnt, p.max_sweeps, sm,
                              n, s, p.flood_blocks_per_sm));
