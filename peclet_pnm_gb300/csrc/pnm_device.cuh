@@ -80,6 +80,25 @@ __device__ __forceinline__ void uf_unite(int* L, int a, int b, unsigned* err) {
   atomicOr(err, ERRF_UF_LIMIT);
 }
 
+// Links the set of `a` with the set of b and returns the root of the merged set as far as this
+// thread knows it. Passing the returned root back as `a` for the next link of the same node
+// keeps its find short (a root, or one hop from one).
+__device__ __forceinline__ int uf_link(int* L, int a, int b, unsigned* err) {
+  for (int it = 0; it < kUfLimit; ++it) {
+    a = uf_find(L, a, err);
+    b = uf_find(L, b, err);
+    if (a == b) return a;
+    const int hi = a > b ? a : b, lo = a > b ? b : a;
+    const int old = atomicMin(&L[hi], lo);
+    if (old == hi) return lo;
+    // hi was linked meanwhile: retry from its new parent
+    a = old;
+    b = lo;
+  }
+  atomicOr(err, ERRF_UF_LIMIT);
+  return a;
+}
+
 // shared-memory variants (tile-local CCL). Parents strictly decrease along a path, so a find
 // ends within the tile size; the limit only bounds the loop.
 constexpr int kUfLimitShared = 1 << 16;

@@ -210,43 +210,38 @@ __global__ void __launch_bounds__(256)
       const int e = p + len - 1;
       const int xs = (c << 5) + p, xe = (c << 5) + e;
       const int head = off + (z * ny + y) * nx + xs;
+      int root = head;  // this run's set: carried from link to link
+      auto link = [&](int t) {
+        root = uf_link(L, root, t, err);
+        ++links;
+      };
       // +x: the node after the run in this row
-      {
-        int t = -1;
-        if (xe == nx - 1) t = node_at(z, y, 0);
-        else if (e == 31 && (__ldg(&vb[(z * ny + y) * ncx + c + 1]) & 1u))
-          t = off + (z * ny + y) * nx + ((c + 1) << 5);
-        if (t >= 0) {
-          uf_unite(L, head, t, err);
-          ++links;
-        }
+      if (xe == nx - 1) {
+        const int t = node_at(z, y, 0);
+        if (t >= 0) link(t);
+      } else if (e == 31 && (__ldg(&vb[(z * ny + y) * ncx + c + 1]) & 1u)) {
+        link(off + (z * ny + y) * nx + ((c + 1) << 5));
       }
 #pragma unroll
       for (int f = 0; f < 4; ++f) {
         const int dy = (f == 0 || f == 3) ? 1 : (f == 1 ? -1 : 0), dz = f == 0 ? 0 : 1;
         const int y2 = wrap1(y + dy, ny), z2 = wrap1(z + dz, nz);
         const int rowb = off + (z2 * ny + y2) * nx;
-        int t = node_at(z2, y2, xs == 0 ? nx - 1 : xs - 1);
-        if (t >= 0) {
-          uf_unite(L, head, t, err);
-          ++links;
-        }
+        const int t0 = node_at(z2, y2, xs == 0 ? nx - 1 : xs - 1);
+        if (t0 >= 0) link(t0);
         const uint32_t w2 = __ldg(&vb[(z2 * ny + y2) * ncx + c]);
         const int hi = e + 1 > 31 ? 31 : e + 1;
         uint32_t sm = (w2 & ~(w2 << 1)) & ((2u << hi) - 1u) & ~((1u << p) - 1u);
         while (sm) {
           const int b = __ffs(sm) - 1;
           sm &= sm - 1;
-          uf_unite(L, head, rowb + (c << 5) + b, err);
-          ++links;
+          link(rowb + (c << 5) + b);
         }
-        t = -1;
-        if (xe + 1 == nx) t = node_at(z2, y2, 0);
-        else if (e == 31 && (__ldg(&vb[(z2 * ny + y2) * ncx + c + 1]) & 1u))
-          t = rowb + ((c + 1) << 5);
-        if (t >= 0) {
-          uf_unite(L, head, t, err);
-          ++links;
+        if (xe + 1 == nx) {
+          const int t = node_at(z2, y2, 0);
+          if (t >= 0) link(t);
+        } else if (e == 31 && (__ldg(&vb[(z2 * ny + y2) * ncx + c + 1]) & 1u)) {
+          link(rowb + ((c + 1) << 5));
         }
       }
     }
