@@ -1049,7 +1049,7 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   const unsigned fgrid = grid_for(n, 256, c.sm_count, 4);
   k_flood_layer2<<<fgrid, 256, 0, s>>>(geo, st->code, key, ulist, &c.d_cnt[CNT_FRONT_SPARE], f0,
                                        &c.d_cnt[CNT_FRONT0]);
-  c.launches += 5;
+  c.launches += 4;
   PNM_CUDA(cudaGetLastError());
 
   // deeper layers: the persistent loop; if a cooperative launch is refused, the same sweeps as
