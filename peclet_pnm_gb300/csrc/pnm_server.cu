@@ -425,7 +425,10 @@ int pnm_server_cancel(pnm_server* s, int64_t ticket) {
   if (!s) return PNM_ERR_ARG;
   std::lock_guard<std::mutex> lk(s->mu);
   Request* r = find(s, ticket);
-  if (!r || r->state != PNM_REQ_QUEUED) return PNM_ERR_ARG;
+  if (!r || r->state != PNM_REQ_QUEUED) {
+    s->last_error = r ? "request is no longer queued (running or finished)" : "unknown ticket";
+    return PNM_ERR_ARG;
+  }
   s->queue.erase(std::find(s->queue.begin(), s->queue.end(), r));
   r->state = PNM_REQ_CANCELLED;
   ++s->cancelled;

@@ -71,7 +71,8 @@ def test_budget_refusal_cancel_and_recovery(gpu):
     big = syn.packing((192, 192, 192), 0.4, mean_r=8.0, seed=4).astype(np.float32)
     budget = int(pnm.batch_plan_bytes([big.shape]) * 1.3)
     assert pnm.batch_plan_bytes([huge.shape]) > budget
-    with pnm.Server(budget_bytes=budget, max_inflight=1) as srv:
+    # one slot, one request per batch: a request submitted while another runs stays queued
+    with pnm.Server(budget_bytes=budget, max_inflight=1, max_batch_volumes=1) as srv:
         t_huge = srv.submit(huge)  # can never fit the budget: refused, the loop goes on
         assert srv.wait(t_huge, 60.0) == PNM_ERR_CAPACITY
         assert srv.state(t_huge)[0] == "failed"
