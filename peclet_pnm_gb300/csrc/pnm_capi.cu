@@ -62,6 +62,16 @@ size_t Workspace::total_bytes() const {
   return t;
 }
 
+Status Ctx::ensure_copy_events(int n) {
+  if (!copy_stream) PNM_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+  while ((int)events.size() < n) {
+    cudaEvent_t e;
+    PNM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    events.push_back(e);
+  }
+  return Status::ok();
+}
+
 Status Ctx::read_counters() {
   PNM_CUDA(cudaMemcpyAsync(h_cnt, d_cnt, CNT_COUNT * sizeof(unsigned), cudaMemcpyDeviceToHost,
                            stream));
@@ -140,11 +150,12 @@ void record(Ctx& c, const pnm::SegState& st, int64_t n_pores, int64_t n_pairs) {
 
 Status do_network(Ctx& c, const float* d_sdf, Dims d, const float* org, const float* spc,
                   pnm_pore* d_pores, int64_t pore_cap, int64_t* n_pores, int32_t* d_seg,
-                  bool want_pairs, int32_t** d_pairs, int64_t* n_pairs) {
+                  bool want_pairs, int32_t** d_pairs, int64_t* n_pairs,
+                  pnm::HostXfer* xfer = nullptr) {
   pnm::SegState st;
-  PNM_TRY(pnm::run_segmentation(c, d_sdf, d, spc, &st));
+  PNM_TRY(pnm::run_segmentation(c, d_sdf, d, spc, &st, false, xfer));
   if (d_pores) PNM_TRY(pnm::run_pores(c, st, org, spc, d_pores, pore_cap, n_pores));
-  PNM_TRY(pnm::run_seg_and_topology(c, st, d_seg, want_pairs, d_pairs, n_pairs));
+  PNM_TRY(pnm::run_seg_and_topology(c, st, d_seg, want_pairs, d_pairs, n_pairs, xfer));
   record(c, st, d_pores ? *n_pores : 0, want_pairs ? *n_pairs : 0);
   return Status::ok();
 }
@@ -196,6 +207,11 @@ void pnm_ctx_destroy(pnm_ctx* ctx) {
   c.ws.release();
   if (c.d_cnt) cudaFree(c.d_cnt);
   if (c.h_cnt) cudaFreeHost(c.h_cnt);
+  if (c.copy_stream) {
+    cudaStreamSynchronize(c.copy_stream);
+    cudaStreamDestroy(c.copy_stream);
+  }
+  for (cudaEvent_t e : c.events) cudaEventDestroy(e);
   if (c.own_stream) cudaStreamDestroy(c.own_stream);
   delete ctx;
 }
@@ -269,17 +285,22 @@ int pnm_segment_volume(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t ny, i
     if (d.n() == 0) return Status::ok();
     if (!sdf || !seg) return Status{PNM_ERR_ARG, "null argument"};
     PNM_TRY(enter(c));
-    const float* d_sdf;
-    PNM_TRY(upload_sdf(c, sdf, d, &d_sdf));
+    float* d_sdf = nullptr;
+    PNM_TRY(c.buf(pnm::S_SDF, d.n(), &d_sdf));
     int32_t* d_seg = nullptr;
     PNM_TRY(c.buf(pnm::S_SEG, d.n(), &d_seg));
     int64_t dummy = 0;
     int32_t* dp = nullptr;
+    pnm::HostXfer xfer;
+    xfer.h_sdf = sdf;
+    xfer.h_seg = seg;
     PNM_TRY(do_network(c, d_sdf, d, spacing_xyz, spacing_xyz, nullptr, 0, &dummy, d_seg, false,
-                       &dp, &dummy));
-    PNM_CUDA(cudaMemcpyAsync(seg, d_seg, d.n() * sizeof(int32_t), cudaMemcpyDeviceToHost,
-                             c.stream));
+                       &dp, &dummy, &xfer));
+    if (!xfer.seg_sent)
+      PNM_CUDA(cudaMemcpyAsync(seg, d_seg, d.n() * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                               c.stream));
     PNM_CUDA(cudaStreamSynchronize(c.stream));
+    if (c.copy_stream) PNM_CUDA(cudaStreamSynchronize(c.copy_stream));
     return Status::ok();
   };
   return finish(ctx, run());
@@ -358,16 +379,20 @@ int pnm_extract_pore_network(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t
       return Status::ok();
     }
     PNM_TRY(enter(c));
-    const float* d_sdf;
-    PNM_TRY(upload_sdf(c, sdf, d, &d_sdf));
+    float* d_sdf = nullptr;
+    PNM_TRY(c.buf(pnm::S_SDF, d.n(), &d_sdf));
     pnm_pore* d_pores = nullptr;
     int32_t* d_seg = nullptr;
     PNM_TRY(c.buf(pnm::S_PORES, kMaxPores, &d_pores));
     PNM_TRY(c.buf(pnm::S_SEG, d.n(), &d_seg));
     int64_t np = 0, m = 0;
     int32_t* d_pairs = nullptr;
+    // the SDF goes up and the labels come back in z-slabs, overlapped with the pipeline
+    pnm::HostXfer xfer;
+    xfer.h_sdf = sdf;
+    xfer.h_seg = seg;
     PNM_TRY(do_network(c, d_sdf, d, origin_xyz, spacing_xyz, d_pores, kMaxPores, &np, d_seg, true,
-                       &d_pairs, &m));
+                       &d_pairs, &m, &xfer));
     np = std::min(np, kMaxPores);
     pnm_pore* hp = static_cast<pnm_pore*>(std::malloc(sizeof(pnm_pore) * (np ? np : 1)));
     int32_t* hq = static_cast<int32_t*>(std::malloc(sizeof(int32_t) * (2 * m + 2)));
@@ -376,13 +401,15 @@ int pnm_extract_pore_network(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t
       std::free(hq);
       return Status{PNM_ERR_INTERNAL, "out of host memory"};
     }
-    PNM_CUDA(cudaMemcpyAsync(seg, d_seg, d.n() * sizeof(int32_t), cudaMemcpyDeviceToHost,
-                             c.stream));
+    if (!xfer.seg_sent)
+      PNM_CUDA(cudaMemcpyAsync(seg, d_seg, d.n() * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                               c.stream));
     if (np) PNM_CUDA(cudaMemcpyAsync(hp, d_pores, np * sizeof(pnm_pore), cudaMemcpyDeviceToHost,
                                      c.stream));
     if (m) PNM_CUDA(cudaMemcpyAsync(hq, d_pairs, 2 * m * sizeof(int32_t), cudaMemcpyDeviceToHost,
                                     c.stream));
     PNM_CUDA(cudaStreamSynchronize(c.stream));
+    if (c.copy_stream) PNM_CUDA(cudaStreamSynchronize(c.copy_stream));
     *pores = hp;
     *n_pores = np;
     *pairs = hq;

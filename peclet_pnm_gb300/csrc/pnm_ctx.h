@@ -83,6 +83,8 @@ struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // host transfers overlapped with the pipeline
+  std::vector<cudaEvent_t> events;     // slab events of those transfers
   Workspace ws;
   unsigned* d_cnt = nullptr;  // CNT_COUNT device counters
   unsigned* h_cnt = nullptr;  // pinned host mirror
@@ -103,7 +105,19 @@ struct Ctx {
     return s;
   }
   Status read_counters();  // synchronises the stream and copies d_cnt -> h_cnt
+  Status ensure_copy_events(int n);  // creates the copy stream and at least n events
 };
+
+// Host buffers of a host-pointer call. With them the stages overlap the transfers with the
+// pipeline: the SDF is uploaded in z-slabs on ctx.copy_stream while the SDF pass runs slab by
+// slab behind it, and the labels go back slab by slab as the seg / topology pass writes them.
+struct HostXfer {
+  const float* h_sdf = nullptr;  // host SDF, uploaded into the stage's device SDF
+  int32_t* h_seg = nullptr;      // host labels (filled from the device labels)
+  bool seg_sent = false;         // set once the label copies are enqueued
+};
+// z-planes per transfer slab (a multiple of 16, the tile and brick depth) for nz planes
+int xfer_slab_planes(int nz);
 
 #ifdef __CUDACC__
 #define PNM_HD __host__ __device__
@@ -140,10 +154,10 @@ struct SegState {
 // Fused SDF pass + CCL + flood + gradient roots + first-appearance renumbering. all_ascent:
 // also compute the ascent pointer of non-pore voxels (network flow's basins need every cell).
 Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st,
-                        bool all_ascent = false);
+                        bool all_ascent = false, HostXfer* xfer = nullptr);
 // Writes seg (if d_seg != null) and the unique sorted label pairs (if want_pairs) from the state.
 Status run_seg_and_topology(Ctx& c, const SegState& st, int32_t* d_seg, bool want_pairs,
-                            int32_t** d_pairs_out, int64_t* n_pairs);
+                            int32_t** d_pairs_out, int64_t* n_pairs, HostXfer* xfer = nullptr);
 // Topology of a caller-provided device seg.
 Status run_topology_of_seg(Ctx& c, const int32_t* d_seg, Dims d, int32_t** d_pairs_out,
                            int64_t* n_pairs);
@@ -156,7 +170,7 @@ void launch_pores_emit(const float* sdf, Dims d, const uint32_t* bits, const uns
                        pnm_pore* out, long long cap, unsigned grid, cudaStream_t s);
 // SDF pass only (for extract_pores alone).
 Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st,
-                    bool all_ascent = false);
+                    bool all_ascent = false, HostXfer* xfer = nullptr);
 
 // ---- network flow (pnm_flow.cu) ------------------------------------------------------------
 struct FlowInputs {

@@ -66,7 +66,9 @@ struct OneVol {
   static constexpr bool kBatch = false;
   Dims d;
   float thr;
+  int base = 0;  // first tile / brick of a launch that covers a z-slab only
   __device__ Box tile(int b, int TXv, int TYv, int TZv, bool /*brick*/) const {
+    b += base;
     Box x;
     x.off = 0;
     x.word0 = 0;

@@ -994,8 +994,13 @@ cudaError_t launch_flood_loop(G geo, const uint8_t* code, int* key, int* L, int*
 }
 }  // namespace
 
+int xfer_slab_planes(int nz) {
+  const int k = std::max(1, std::min(8, (nz + 15) / 16));  // up to 8 slabs
+  return ((nz + k - 1) / k + 15) / 16 * 16;
+}
+
 Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st,
-                    bool all_ascent) {
+                    bool all_ascent, HostXfer* xfer) {
   const long long n = d.n();
   const long long words = (n + 31) / 32;
   st->d = d;
@@ -1008,27 +1013,56 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
   st->n_words = (long long)d.nz * d.ny * ((d.nx + 31) / 32);
   PNM_TRY(c.buf(S_EDGES, st->n_words, &st->mbits));
   PNM_TRY(c.buf(S_NXT, n, &st->nxt));
-  const OneVol geo{d, marker_threshold(spacing)};
-  const unsigned tiles = (unsigned)boxes_of(d, TX, TY, TZ_PLAIN);
-  if (all_ascent)
-    k_sdf_pass<true, OneVol, TZ_PLAIN><<<tiles, TX * TY, 0, c.stream>>>(
-        d_sdf, geo, st->code, st->nxt, L, st->peakbits, st->mbits);
-  else
-    k_sdf_pass<false, OneVol, TZ_PLAIN><<<tiles, TX * TY, 0, c.stream>>>(
-        d_sdf, geo, st->code, st->nxt, L, st->peakbits, st->mbits);
-  ++c.launches;
+  OneVol geo{d, marker_threshold(spacing)};
+  auto launch = [&](unsigned tiles) {
+    if (all_ascent)
+      k_sdf_pass<true, OneVol, TZ_PLAIN><<<tiles, TX * TY, 0, c.stream>>>(
+          d_sdf, geo, st->code, st->nxt, L, st->peakbits, st->mbits);
+    else
+      k_sdf_pass<false, OneVol, TZ_PLAIN><<<tiles, TX * TY, 0, c.stream>>>(
+          d_sdf, geo, st->code, st->nxt, L, st->peakbits, st->mbits);
+    ++c.launches;
+  };
+  if (!xfer || !xfer->h_sdf) {
+    launch((unsigned)boxes_of(d, TX, TY, TZ_PLAIN));
+  } else {
+    // upload in z-slabs (the last plane first: the first slab's periodic halo), and run the
+    // SDF pass of each slab once its own planes and the next slab's first plane have arrived
+    const int zs = xfer_slab_planes(d.nz), k = (d.nz + zs - 1) / zs;
+    const long long plane = (long long)d.nx * d.ny;
+    float* dst = const_cast<float*>(d_sdf);
+    PNM_TRY(c.ensure_copy_events(2 * k + 2));
+    PNM_CUDA(cudaEventRecord(c.events[2 * k], c.stream));  // the device buffer is free
+    PNM_CUDA(cudaStreamWaitEvent(c.copy_stream, c.events[2 * k], 0));
+    PNM_CUDA(cudaMemcpyAsync(dst + (d.nz - 1) * plane, xfer->h_sdf + (d.nz - 1) * plane,
+                             plane * sizeof(float), cudaMemcpyHostToDevice, c.copy_stream));
+    for (int i = 0; i < k; ++i) {
+      const int z0 = i * zs, z1 = std::min(d.nz, z0 + zs);
+      PNM_CUDA(cudaMemcpyAsync(dst + z0 * plane, xfer->h_sdf + z0 * plane,
+                               (z1 - z0) * plane * sizeof(float), cudaMemcpyHostToDevice,
+                               c.copy_stream));
+      PNM_CUDA(cudaEventRecord(c.events[i], c.copy_stream));
+    }
+    const long long tpp = (long long)((d.nx + TX - 1) / TX) * ((d.ny + TY - 1) / TY);
+    for (int i = 0; i < k; ++i) {
+      const int z0 = i * zs, z1 = std::min(d.nz, z0 + zs);
+      PNM_CUDA(cudaStreamWaitEvent(c.stream, c.events[std::min(i + 1, k - 1)], 0));
+      geo.base = (int)(z0 / TZ_PLAIN * tpp);
+      launch((unsigned)(((z1 - z0 + TZ_PLAIN - 1) / TZ_PLAIN) * tpp));
+    }
+  }
   PNM_CUDA(cudaGetLastError());
   st->idtab = L;
   return Status::ok();
 }
 
 Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st,
-                        bool all_ascent) {
+                        bool all_ascent, HostXfer* xfer) {
   const long long n = d.n();
   const long long words = (n + 31) / 32;
   cudaStream_t s = c.stream;
   PNM_CUDA(cudaMemsetAsync(c.d_cnt, 0, CNT_COUNT * sizeof(unsigned), s));
-  PNM_TRY(run_sdf_pass(c, d_sdf, d, spacing, st, all_ascent));
+  PNM_TRY(run_sdf_pass(c, d_sdf, d, spacing, st, all_ascent, xfer));
   const OneVol geo{d, marker_threshold(spacing)};
   int* L = st->idtab;
   int *key, *keylist, *f0, *f1, *tmp, *ulist;
@@ -1122,7 +1156,7 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
 namespace {
 Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int32_t* d_seg_in,
                   int32_t* d_seg_out, bool want_pairs, long long cap_hint, int32_t** d_pairs_out,
-                  int64_t* n_pairs) {
+                  int64_t* n_pairs, HostXfer* xfer = nullptr) {
   cudaStream_t s = c.stream;
   const long long n = d.n();
   long long cap = 4096;
@@ -1138,15 +1172,40 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
     PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_ERR], 0, sizeof(unsigned), s));
     PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_FLOW_SPARE1], 0, sizeof(unsigned), s));
     const unsigned g = (unsigned)boxes_of(d, STX, STY, STZ);
-    const OneVol geo{d, 0.0f};
-    if (from_keys)
-      k_seg_topo<<<g, STX * STY, 0, s>>>(geo, KeyLabels{st->key, st->idtab}, d_seg_out,
+    OneVol geo{d, 0.0f};
+    // labels already on their way to the host (an earlier attempt) are not written again
+    int32_t* seg_out = (xfer && xfer->seg_sent) ? nullptr : d_seg_out;
+    if (from_keys && xfer && xfer->h_seg && seg_out) {
+      // z-slabs of bricks; each slab's labels go to the host while the next slabs and the
+      // pair stages run
+      const int zs = xfer_slab_planes(d.nz), k = (d.nz + zs - 1) / zs;
+      const long long plane = (long long)d.nx * d.ny;
+      const long long bpp = (long long)((d.nx + STX - 1) / STX) * ((d.ny + STY - 1) / STY);
+      PNM_TRY(c.ensure_copy_events(2 * k + 2));
+      for (int i = 0; i < k; ++i) {
+        const int z0 = i * zs, z1 = std::min(d.nz, z0 + zs);
+        geo.base = (int)(z0 / STZ * bpp);
+        k_seg_topo<<<(unsigned)(((z1 - z0 + STZ - 1) / STZ) * bpp), STX * STY, 0, s>>>(
+            geo, KeyLabels{st->key, st->idtab}, seg_out, want_pairs ? 1 : 0, table,
+            (uint64_t)(cap - 1), c.d_cnt, range);
+        ++c.launches;
+        PNM_CUDA(cudaEventRecord(c.events[k + i], s));
+        PNM_CUDA(cudaStreamWaitEvent(c.copy_stream, c.events[k + i], 0));
+        PNM_CUDA(cudaMemcpyAsync(xfer->h_seg + z0 * plane, seg_out + z0 * plane,
+                                 (z1 - z0) * plane * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                 c.copy_stream));
+      }
+      xfer->seg_sent = true;
+    } else if (from_keys) {
+      k_seg_topo<<<g, STX * STY, 0, s>>>(geo, KeyLabels{st->key, st->idtab}, seg_out,
                                          want_pairs ? 1 : 0, table, (uint64_t)(cap - 1), c.d_cnt,
                                          range);
-    else
-      k_seg_topo<<<g, STX * STY, 0, s>>>(geo, SegLabels{d_seg_in}, d_seg_out, want_pairs ? 1 : 0,
+      ++c.launches;
+    } else {
+      k_seg_topo<<<g, STX * STY, 0, s>>>(geo, SegLabels{d_seg_in}, seg_out, want_pairs ? 1 : 0,
                                          table, (uint64_t)(cap - 1), c.d_cnt, range);
-    ++c.launches;
+      ++c.launches;
+    }
     PNM_CUDA(cudaGetLastError());
     if (!want_pairs) return Status::ok();
     PNM_TRY(c.read_counters());
@@ -1185,10 +1244,11 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
 }  // namespace
 
 Status run_seg_and_topology(Ctx& c, const SegState& st, int32_t* d_seg, bool want_pairs,
-                            int32_t** d_pairs_out, int64_t* n_pairs) {
+                            int32_t** d_pairs_out, int64_t* n_pairs, HostXfer* xfer) {
   const long long labels = (long long)st.n_pore_labels + st.n_solid_labels + 2;
   const long long hint = std::min<long long>(std::max<long long>(64 * labels, 4096), 3 * st.d.n() + 64);
-  return emit_pairs(c, st.d, true, &st, nullptr, d_seg, want_pairs, hint, d_pairs_out, n_pairs);
+  return emit_pairs(c, st.d, true, &st, nullptr, d_seg, want_pairs, hint, d_pairs_out, n_pairs,
+                    xfer);
 }
 
 Status run_topology_of_seg(Ctx& c, const int32_t* d_seg, Dims d, int32_t** d_pairs_out,
