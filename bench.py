@@ -57,6 +57,8 @@ def parse():
                     help="skip the ragged 96-volume batched-vs-plain measurement")
     ap.add_argument("--no-served", action="store_true",
                     help="skip the Poisson serving measurement")
+    ap.add_argument("--no-flow", action="store_true",
+                    help="skip the 256^3 float64 extract_network_flow measurement")
     ap.add_argument("--batch-volumes", type=int, default=96)
     ap.add_argument("--serve-requests", type=int, default=600)
     return ap.parse_args()
@@ -332,6 +334,65 @@ def batched_bench(args, dev):
     return out
 
 
+def flow_bench(args, dev):
+    """extract_network_flow on a 256^3 float64 packing (seed 3) with u, v, w, p = 32 random Fourier
+    modes (|k| <= 8, amplitude 1e-3, seed 4) zeroed in solid, openness clamp(0.5 + face SDF, 0, 1),
+    grad_p_zyx = [0, 0, -1e-4]; through the host C ABI (host SDF and fields in, host results out,
+    the reference binding's call). Check: the pore residuals of a closed periodic network sum to
+    zero (every throat flux leaves one pore and enters another)."""
+    import torch
+
+    import peclet_pnm_gb300 as pnm
+    from peclet_pnm_gb300 import _capi
+    from peclet_pnm_gb300 import synthetic as syn
+
+    n = 256
+    sdf = syn.packing((n, n, n), 0.4, seed=3, dtype=np.float64, device=dev)
+    fields = syn.fourier_fields_device(sdf)
+    h_sdf = torch.empty((n, n, n), dtype=torch.float32, pin_memory=True)
+    h_sdf.copy_(sdf.to(torch.float32))
+    hf = []
+    for f in fields:
+        h = torch.empty((n, n, n), dtype=torch.float64, pin_memory=True)
+        h.copy_(f)
+        hf.append(h)
+    del sdf, fields
+    torch.cuda.empty_cache()
+    ctx = pnm.Context(dev.index)
+    o = np.zeros(3, np.float32)
+    s = np.ones(3, np.float32)
+    g = np.array([0.0, 0.0, -1e-4], np.float64)[::-1].copy()  # xyz
+    res = _capi._P(_capi.PnmFlowResult)()
+
+    def call():
+        ctx.check(_capi.pnm_extract_network_flow(
+            ctx.h, ctypes.c_void_p(h_sdf.data_ptr()), n, n, n, _capi.as_ptr(o), _capi.as_ptr(s),
+            *[ctypes.c_void_p(h.data_ptr()) for h in hf], _capi.as_ptr(g), ctypes.byref(res)))
+
+    for _ in range(2):
+        call()
+        _capi.pnm_flow_result_free(res)
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        call()
+        ts.append(time.perf_counter() - t0)
+        r = res.contents
+        npo, nth = int(r.n_pores), int(r.n_throats)
+        resid = np.ctypeslib.as_array(r.pore_residual, (npo,)).copy() if npo else np.zeros(0)
+        flow = np.ctypeslib.as_array(r.throat_flow, (nth,)).copy() if nth else np.zeros(0)
+        _capi.pnm_flow_result_free(res)
+    t = float(np.median(ts))
+    scale = float(np.abs(flow).sum()) or 1.0
+    ctx.close()
+    return {"workload": "extract_network_flow 256^3 float64 packing (seed 3), 32-mode Fourier "
+                        "u,v,w,p (seed 4), openness from face SDF, grad_p_zyx [0,0,-1e-4]",
+            "e2e": {"value": n ** 3 / t / 1e9, "unit": "Gvoxel/s", "ms_per_step": t * 1e3,
+                    "h2d_bytes_per_step": 4 * n ** 3 + 7 * 8 * n ** 3},
+            "pores": npo, "throats": nth,
+            "residual_sum_over_flux": float(abs(resid.sum())) / scale}
+
+
 def served_bench(args, dev):
     """Poisson requests (rate 200/s, seed 6), cubic edges log-uniform in [32, 384], SDFs in pinned
     host memory: 64 distinct request volumes cut from two 384^3 packings, cycled through the
@@ -593,6 +654,8 @@ def ours(args, rank, world, local_rank):
         result["batched"] = batched_bench(args, dev)
     if rank == 0 and world == 1 and not args.no_served:
         result["served"] = served_bench(args, dev)
+    if rank == 0 and world == 1 and not args.no_flow:
+        result["flow"] = flow_bench(args, dev)
     if rank == 0:
         print(json.dumps(result), flush=True)
 

@@ -277,6 +277,46 @@ def fourier_fields(sdf_zyx: np.ndarray, modes: int = 32, kmax: int = 8, amplitud
     return tuple(out)
 
 
+def fourier_fields_device(sdf, modes: int = 32, kmax: int = 8, amplitude: float = 1e-3,
+                          seed: int = 4):
+    """fourier_fields evaluated in torch on the SDF tensor's device (float64): the same modes,
+    phases and directions (same random stream), for volumes where the host version is slow."""
+    import torch
+
+    dev = sdf.device
+    sdf = sdf.to(torch.float64)
+    nz, ny, nx = sdf.shape
+    rng = np.random.default_rng(seed)
+    z = torch.arange(nz, dtype=torch.float64, device=dev)[:, None, None] / nz
+    y = torch.arange(ny, dtype=torch.float64, device=dev)[None, :, None] / ny
+    x = torch.arange(nx, dtype=torch.float64, device=dev)[None, None, :] / nx
+
+    def one(is_vec_comp: bool):
+        acc = torch.zeros((nz, ny, nx), dtype=torch.float64, device=dev)
+        m = 0
+        while m < modes:
+            k = rng.integers(-kmax, kmax + 1, size=3)
+            if not (0 < np.sqrt((k * k).sum()) <= kmax):
+                continue
+            ph = rng.uniform(0.0, 2 * np.pi)
+            a = amplitude * (rng.normal() if is_vec_comp else 1.0)
+            acc += a * torch.sin(2 * np.pi * (float(k[0]) * x + float(k[1]) * y + float(k[2]) * z)
+                                 + ph)
+            m += 1
+        return acc
+
+    solid = sdf <= 0.0
+    out = []
+    for comp in range(4):
+        f = one(comp < 3)
+        f[solid] = 0.0
+        out.append(f.contiguous())
+    for ax in (2, 1, 0):
+        face = 0.5 * (torch.roll(sdf, 1, dims=ax) + sdf)
+        out.append(torch.clamp(0.5 + face, 0.0, 1.0).contiguous())
+    return tuple(out)
+
+
 def batch_shapes(count: int = 96, edges=(48, 64, 96, 128, 160, 192), seed: int = 5):
     """Per-volume (nz, ny, nx) and porosity of the ragged batch: edges drawn per axis, seed+i."""
     out = []
