@@ -39,35 +39,45 @@ struct I128 {
   unsigned long long lo;
   long long hi;
 };
+// trunc(x * 2^scale) as a 128-bit two's-complement integer, from the bits of x (integer
+// instructions only: GB300's FP64 rate is low); 0 for zero, inf and NaN. Exact: the shift of the
+// 53-bit significand is clamped at 73, which the chosen scales never reach.
 __device__ __forceinline__ I128 to_fixed(double x, int scale) {
   I128 r{0ull, 0ll};
-  if (x == 0.0 || !isfinite(x)) return r;
-  const double y = scalbn(x, scale);  // exact power-of-two scaling
-  const double a = fabs(y);
-  unsigned long long mlo;
-  long long mhi;
-  if (a < 9223372036854775808.0) {  // < 2^63
-    mlo = (unsigned long long)a;    // truncation toward zero
-    mhi = 0;
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((bits >> 52) & 0x7ffull);
+  unsigned long long m = bits & ((1ull << 52) - 1ull);
+  if (e == 0x7ff || (e == 0 && m == 0)) return r;
+  int sh;
+  if (e == 0) {
+    sh = 1 - 1075 + scale;  // subnormal: no implicit bit
   } else {
-    int e;
-    const double fr = frexp(a, &e);  // a = fr * 2^e, fr in [0.5, 1)
-    const unsigned long long m = (unsigned long long)scalbn(fr, 53);  // 53-bit integer mantissa
-    const int sh = min(e - 53, 73);  // >= 10 here; < 42 by the chosen scale (clamp: no UB)
+    m |= 1ull << 52;
+    sh = e - 1075 + scale;
+  }
+  unsigned long long mlo, mhi;
+  if (sh >= 0) {
+    sh = min(sh, 73);
     if (sh >= 64) {
       mlo = 0;
-      mhi = (long long)(m << (sh - 64));
+      mhi = m << (sh - 64);
+    } else if (sh == 0) {
+      mlo = m;
+      mhi = 0;
     } else {
       mlo = m << sh;
-      mhi = (long long)(m >> (64 - sh));
+      mhi = m >> (64 - sh);
     }
+  } else {
+    mlo = -sh >= 64 ? 0ull : (m >> -sh);  // truncation toward zero of the magnitude
+    mhi = 0;
   }
-  if (y < 0) {  // two's complement negate
+  if (bits >> 63) {  // two's complement negate
     mlo = ~mlo + 1ull;
-    mhi = ~mhi + (mlo == 0 ? 1 : 0);
+    mhi = ~mhi + (mlo == 0 ? 1ull : 0ull);
   }
   r.lo = mlo;
-  r.hi = mhi;
+  r.hi = (long long)mhi;
   return r;
 }
 __device__ __forceinline__ I128 add128(I128 a, I128 b) {
@@ -83,19 +93,33 @@ __device__ __forceinline__ void atomic_add128(unsigned long long* acc, I128 v) {
   const unsigned long long hi = (unsigned long long)v.hi + carry;
   if (hi) atomicAdd(&acc[1], hi);
 }
-// Sums the I128 values of the lanes sharing `target` (>= 0) and lets the lowest such lane add the
-// group total to acc[2*target]. Exact, so the grouping does not affect the result.
-__device__ __forceinline__ void warp_accumulate(unsigned long long* acc, int target, I128 v) {
-  const unsigned peers = __match_any_sync(0xffffffffu, target);
-  I128 s{0ull, 0ll};
-#pragma unroll 4
-  for (int j = 0; j < 32; ++j) {
-    I128 o;
-    o.lo = __shfl_sync(0xffffffffu, v.lo, j);
-    o.hi = __shfl_sync(0xffffffffu, v.hi, j);
-    if ((peers >> j) & 1u) s = add128(s, o);
+// Adds each lane's I128 values to acc[k][2*target] for target >= 0. Lanes are summed over runs of
+// consecutive lanes with the same target (a segmented scan: 5 shuffle steps), and the last lane of
+// each run issues the atomics, so a warp needs one atomic per run instead of one per lane. The
+// sums are exact integers, so how lanes are grouped never changes a result.
+template <int N>
+__device__ __forceinline__ void warp_accumulate(unsigned long long* const (&acc)[N], int target,
+                                                I128 (&v)[N]) {
+  if (!__any_sync(0xffffffffu, target >= 0)) return;  // no face of this kind in the warp
+  const int lane = (int)lane_id();
+  const int prev = __shfl_up_sync(0xffffffffu, target, 1);
+  const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev != target);
+  const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));  // this lane's run start
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      I128 u;
+      u.lo = __shfl_up_sync(0xffffffffu, v[k].lo, o);
+      u.hi = __shfl_up_sync(0xffffffffu, v[k].hi, o);
+      if (lane - o >= start) v[k] = add128(v[k], u);
+    }
   }
-  if (target >= 0 && (__ffs(peers) - 1) == (int)lane_id()) atomic_add128(&acc[2 * (long long)target], s);
+  const int next = __shfl_down_sync(0xffffffffu, target, 1);
+  if (target >= 0 && (lane == 31 || next != target)) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) atomic_add128(&acc[k][2 * (long long)target], v[k]);
+  }
 }
 __device__ __forceinline__ double from_fixed(unsigned long long lo, long long hi, int scale) {
   const bool neg = hi < 0;
@@ -483,6 +507,8 @@ struct FluxParams {
   double area[3];
   double L[3];
   float o[3], s[3];
+  int N[3];
+  int fast[3];     // per axis: |origin| + L small enough for the integer minimum-image test
   int sq, sa, sc;  // fixed-point scales: fluxes/residuals, areas, centroid moments
 };
 
@@ -548,19 +574,31 @@ __global__ void __launch_bounds__(256)
                                            __dmul_rn(__dadd_rn((double)ci[a2], dd == a2 ? 0.5 : 0.0), sp));
               const double pcv = __dadd_rn((double)P.o[a2], __dmul_rn((double)pi[a2], sp));
               double dv = __dsub_rn(fpv, pcv);
-              dv = __dsub_rn(dv, __dmul_rn(P.L[a2], round(__ddiv_rn(dv, P.L[a2]))));
+              // minimum image: k = round(dv / L). In half-voxel units the exact difference is
+              // t2 = 2 (c - p) + h; away from |t2| ~ N the rounding errors (< 2^-13 voxel when
+              // P.fast[a2]) cannot move dv/L across +-0.5, so k follows from integers
+              const int t2 = 2 * (ci[a2] - pi[a2]) + (dd == a2 ? 1 : 0);
+              const int at = t2 < 0 ? -t2 : t2;
+              if (!P.fast[a2] || (at > P.N[a2] - 2 && at < P.N[a2] + 2)) {
+                dv = __dsub_rn(dv, __dmul_rn(P.L[a2], round(__ddiv_rn(dv, P.L[a2]))));
+              } else if (at >= P.N[a2] + 2) {
+                dv = __dsub_rn(dv, __dmul_rn(P.L[a2], t2 < 0 ? -1.0 : 1.0));
+              }
               vC[a2] = to_fixed(__dmul_rn(w0, dv), P.sc);
             }
           }
         }
       }
-      warp_accumulate(accR, ta, vq);
-      warp_accumulate(accR, tb, vnq);
-      warp_accumulate(accQ, ts, vQ);
-      warp_accumulate(accA, ts, vA);
-      warp_accumulate(accCx, ts, vC[0]);
-      warp_accumulate(accCy, ts, vC[1]);
-      warp_accumulate(accCz, ts, vC[2]);
+      {
+        unsigned long long* const r1[1] = {accR};
+        I128 a1[1] = {vq};
+        warp_accumulate<1>(r1, ta, a1);
+        I128 b1[1] = {vnq};
+        warp_accumulate<1>(r1, tb, b1);
+        unsigned long long* const r5[5] = {accQ, accA, accCx, accCy, accCz};
+        I128 v5[5] = {vQ, vA, vC[0], vC[1], vC[2]};
+        warp_accumulate<5>(r5, ts, v5);
+      }
     }
   }
 }
@@ -771,6 +809,11 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
     P.L[a] = (double)N[a] * spacing[a];  // :876
     P.o[a] = origin[a];
     P.s[a] = spacing[a];
+    P.N[a] = N[a];
+    // face and peak coordinates carry rounding errors below 4 ulp of |o| + L; the integer test
+    // keeps a one-voxel margin, so it applies while that is far below a voxel
+    P.fast[a] = (std::fabs((double)origin[a]) + P.L[a]) < std::ldexp((double)spacing[a], 40) &&
+                N[a] >= 4;
     Lmax = std::max(Lmax, P.L[a]);
   }
   P.sq = fixed_scale(bq);
