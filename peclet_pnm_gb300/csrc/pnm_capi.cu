@@ -474,19 +474,24 @@ int pnm_extract_network_flow(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t
     if (3 * d.n() > (long long)INT_MAX - 8)
       return Status{PNM_ERR_SHAPE, "volume too large for network flow: 3*nx*ny*nz must be < 2^31"};
     PNM_TRY(enter(c));
-    const float* d_sdf;
-    PNM_TRY(upload_sdf(c, sdf, d, &d_sdf));
+    float* d_sdf = nullptr;
+    PNM_TRY(c.buf(pnm::S_SDF, d.n(), &d_sdf));
     const size_t nb = d.n() * sizeof(double);
     const double* hf[7] = {u, v, w, p, ox, oy, oz};
     const int slots[7] = {pnm::S_U, pnm::S_V, pnm::S_W, pnm::S_P, pnm::S_OX, pnm::S_OY, pnm::S_OZ};
     double* df[7] = {};
+    // the SDF goes up in slabs ahead of the SDF pass; the fields follow on the copy stream and
+    // arrive while the segmentation runs (only the flow stage reads them)
+    pnm::HostXfer xfer;
+    xfer.h_sdf = sdf;
     for (int i = 0; i < 7; ++i) {
       if (!hf[i]) continue;
       PNM_TRY(c.buf(slots[i], d.n(), &df[i]));
-      PNM_CUDA(cudaMemcpyAsync(df[i], hf[i], nb, cudaMemcpyHostToDevice, c.stream));
+      xfer.extra.push_back({df[i], hf[i], nb});
     }
     pnm::SegState st;
-    PNM_TRY(pnm::run_segmentation(c, d_sdf, d, spacing_xyz, &st, /*all_ascent=*/true));
+    PNM_TRY(pnm::run_segmentation(c, d_sdf, d, spacing_xyz, &st, /*all_ascent=*/true, &xfer));
+    if (xfer.extra_done) PNM_CUDA(cudaStreamWaitEvent(c.stream, xfer.extra_done, 0));
     pnm::FlowInputs in{df[0], df[1], df[2], df[3], df[4], df[5], df[6],
                        {grad_p_xyz[0], grad_p_xyz[1], grad_p_xyz[2]}};
     pnm::FlowOutputsHost o;

@@ -115,6 +115,15 @@ struct HostXfer {
   const float* h_sdf = nullptr;  // host SDF, uploaded into the stage's device SDF
   int32_t* h_seg = nullptr;      // host labels (filled from the device labels)
   bool seg_sent = false;         // set once the label copies are enqueued
+  // further host -> device copies, queued behind the SDF slabs (they run during the pipeline);
+  // extra_done is recorded on the copy stream after them
+  struct Copy {
+    void* dst;
+    const void* src;
+    size_t bytes;
+  };
+  std::vector<Copy> extra;
+  cudaEvent_t extra_done = nullptr;
 };
 // z-planes per transfer slab (a multiple of 16, the tile and brick depth) for nz planes
 int xfer_slab_planes(int nz);

@@ -1043,6 +1043,13 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
                                c.copy_stream));
       PNM_CUDA(cudaEventRecord(c.events[i], c.copy_stream));
     }
+    if (!xfer->extra.empty()) {
+      for (const auto& cp : xfer->extra)
+        PNM_CUDA(cudaMemcpyAsync(cp.dst, cp.src, cp.bytes, cudaMemcpyHostToDevice,
+                                 c.copy_stream));
+      PNM_CUDA(cudaEventRecord(c.events[2 * k + 1], c.copy_stream));
+      xfer->extra_done = c.events[2 * k + 1];
+    }
     const long long tpp = (long long)((d.nx + TX - 1) / TX) * ((d.ny + TY - 1) / TY);
     for (int i = 0; i < k; ++i) {
       const int z0 = i * zs, z1 = std::min(d.nz, z0 + zs);
