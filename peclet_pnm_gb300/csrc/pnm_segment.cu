@@ -269,6 +269,7 @@ __global__ void __launch_bounds__(RTX* RTY)
     k_resolve(G geo, const uint8_t* __restrict__ code, const int* __restrict__ nxt, int* L,
               int* __restrict__ key, int* __restrict__ keylist, unsigned* cnt) {
   __shared__ uint8_t cb[RTZ][RTY][RTX];
+  __shared__ short nl[RTZ * RTY * RTX];  // in-brick ascent successor (local index), -1: leaves
   unsigned* err = &cnt[CNT_ERR];
   const Box bx = geo.tile(blockIdx.x, RTX, RTY, RTZ, true);
   const int off = bx.off, nx = bx.nx, ny = bx.ny, nz = bx.nz;
@@ -278,9 +279,16 @@ __global__ void __launch_bounds__(RTX* RTY)
   const int lane = threadIdx.x & 31, ty = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < RTX * RTY * RTZ; i += RTX * RTY) {
     const int lx = i % RTX, ly = (i / RTX) % RTY, lz = i / (RTX * RTY);
-    cb[lz][ly][lx] = (lx < TXe && ly < TYe && lz < TZe)
-                         ? __ldg(&code[off + (Z0 + lz) * nxy + (Y0 + ly) * nx + X0 + lx])
-                         : make_code(kSelf, CLS_ZERO, false);
+    const uint8_t cc = (lx < TXe && ly < TYe && lz < TZe)
+                           ? __ldg(&code[off + (Z0 + lz) * nxy + (Y0 + ly) * nx + X0 + lx])
+                           : make_code(kSelf, CLS_ZERO, false);
+    cb[lz][ly][lx] = cc;
+    const int dk = code_dir(cc);
+    const int x2 = lx + dk % 3 - 1, y2 = ly + (dk / 3) % 3 - 1, z2 = lz + dk / 9 - 1;
+    nl[i] = dk == kSelf ? (short)i
+            : (x2 < 0 || x2 >= TXe || y2 < 0 || y2 >= TYe || z2 < 0 || z2 >= TZe)
+                ? (short)-1
+                : (short)((z2 * RTY + y2) * RTX + x2);
   }
   __syncthreads();
   const bool inxy = lane < TXe && ty < TYe;
@@ -295,21 +303,19 @@ __global__ void __launch_bounds__(RTX* RTY)
       if (cls == CLS_MARKER) {
         par = ld_relaxed(&L[v]);
       } else if (cls == CLS_PORE) {
-        int x = lane, y = ty, z = tz, moves = 0;
+        int li = (tz * RTY + ty) * RTX + lane, moves = 0;
         bool root = false;
-        while (moves < 512) {  // inside the brick: direction bits
-          const int dk = code_dir(cb[z][y][x]);
-          if (dk == kSelf) {
+        while (moves < 512) {  // inside the brick: the successor table
+          const int nli = nl[li];
+          if (nli == li) {
             root = true;
             break;
           }
-          const int x2 = x + dk % 3 - 1, y2 = y + (dk / 3) % 3 - 1, z2 = z + dk / 9 - 1;
-          if (x2 < 0 || x2 >= TXe || y2 < 0 || y2 >= TYe || z2 < 0 || z2 >= TZe) break;
-          x = x2;
-          y = y2;
-          z = z2;
+          if (nli < 0) break;  // the next move leaves the brick (or wraps)
+          li = nli;
           ++moves;
         }
+        const int x = li % RTX, y = (li / RTX) % RTY, z = li / (RTX * RTY);
         int cur = off + (Z0 + z) * nxy + (Y0 + y) * nx + X0 + x;
         if (!root) {  // left the brick: the global pointers for the remaining moves
           for (; moves < 512; ++moves) {
