@@ -67,6 +67,7 @@ enum Slot : int {
   S_U, S_V, S_W, S_P, S_OX, S_OY, S_OZ, S_FLOWLAB, S_FBITS, S_FCORE, S_FPREF, S_FID, S_FPAIR,
   S_FPAR, S_FFILM, S_FMINCORE, S_FLABEL, S_ROOTFLAG, S_SLOTOF, S_PEAK, S_NPORES_OUT,
   S_PPRES, S_REC, S_ACC, S_TDP, S_THROATS, S_MAXBITS, S_FLOWOUT, S_ULIST, S_EDGES, S_NXT, S_STEPS,
+  S_COORD,
   S_COUNT
 };
 

@@ -503,10 +503,19 @@ __global__ void k_slots(long long nt, const uint64_t* __restrict__ keys,
   }
 }
 
+// Face / cell-centre coordinates along one axis: F[2c + h] = o + (c + h/2) * s with the
+// reference's roundings (double of the float origin and spacing, :876-900).
+__global__ void k_coord_table(double* __restrict__ F, int n, float o, float s) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * n; i += gridDim.x * blockDim.x)
+    F[i] = __dadd_rn((double)o, __dmul_rn(__dadd_rn((double)(i >> 1), (i & 1) ? 0.5 : 0.0),
+                                          (double)s));
+}
+
 struct FluxParams {
   double area[3];
   double L[3];
   float o[3], s[3];
+  const double* F[3];  // per axis: F[2c + h] = o + (c + h/2) s, rounded as the reference does
   int N[3];
   int fast[3];     // per axis: |origin| + L small enough for the integer minimum-image test
   int sq, sa, sc;  // fixed-point scales: fluxes/residuals, areas, centroid moments
@@ -569,10 +578,8 @@ __global__ void __launch_bounds__(256)
             const int pi[3] = {pc.x, pc.y, pc.z};
 #pragma unroll
             for (int a2 = 0; a2 < 3; ++a2) {
-              const double sp = (double)P.s[a2];
-              const double fpv = __dadd_rn((double)P.o[a2],
-                                           __dmul_rn(__dadd_rn((double)ci[a2], dd == a2 ? 0.5 : 0.0), sp));
-              const double pcv = __dadd_rn((double)P.o[a2], __dmul_rn((double)pi[a2], sp));
+              const double fpv = __ldg(&P.F[a2][2 * ci[a2] + (dd == a2 ? 1 : 0)]);
+              const double pcv = __ldg(&P.F[a2][2 * pi[a2]]);
               double dv = __dsub_rn(fpv, pcv);
               // minimum image: k = round(dv / L). In half-voxel units the exact difference is
               // t2 = 2 (c - p) + h; away from |t2| ~ N the rounding errors (< 2^-13 voxel when
@@ -819,6 +826,18 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
   P.sq = fixed_scale(bq);
   P.sa = fixed_scale(bw);
   P.sc = fixed_scale(bw * (Lmax + 1.0));
+  {
+    double* F = nullptr;
+    PNM_TRY(c.buf(S_COORD, 2 * ((long long)N[0] + N[1] + N[2]), &F));
+    long long at = 0;
+    for (int a = 0; a < 3; ++a) {
+      P.F[a] = F + at;
+      k_coord_table<<<(unsigned)std::min<long long>((2 * N[a] + 255) / 256, 1024), 256, 0, s>>>(
+          F + at, N[a], P.o[a], P.s[a]);
+      ++c.launches;
+      at += 2 * (long long)N[a];
+    }
+  }
   const long long nacc = (long long)np + 5 * std::max<long long>(nt, 1);
   unsigned long long* acc;
   PNM_TRY(c.buf(S_REC, 2 * nacc, &acc));
