@@ -514,7 +514,7 @@ def served_bench(args, dev):
         "offered_gvoxel_per_s": vox / arrivals[-1] / 1e9,
         "served": {"p50_ms": sp["p50_ms"], "p99_ms": sp["p99_ms"], "mean_ms": sp["mean_ms"],
                    "gvoxel_per_s": sp["gvoxel_per_s"], "batches": int(sp["batches"]),
-                   "requests": int(sp["completed"]),
+                   "requests": int(sp["completed"]), "batch_reuse": int(sp["cache_hits"]),
                    "peak_device_gb": sp["peak_bytes"] / 1e9},
         "plain": {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                   "mean_ms": float(lat.mean()), "gvoxel_per_s": vox / plain_span / 1e9},

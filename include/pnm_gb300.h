@@ -265,6 +265,8 @@ typedef struct {
   double p50_ms, p99_ms, mean_ms, max_ms; /* submit -> results resident, completed requests */
   double busy_s;             /* first submit -> last completion */
   double gvoxel_per_s;       /* voxels_completed / busy_s / 1e9 */
+  int64_t cache_hits;        /* batches that reused an idle batch of the same shapes */
+  int64_t cached;            /* idle batches held now */
 } pnm_server_stats;
 
 #define PNM_REQ_QUEUED 0

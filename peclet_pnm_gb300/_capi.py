@@ -144,7 +144,7 @@ class PnmServerStats(ctypes.Structure):
                 ("peak_bytes", _i64), ("voxels_completed", _i64), ("p50_ms", ctypes.c_double),
                 ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
                 ("max_ms", ctypes.c_double), ("busy_s", ctypes.c_double),
-                ("gvoxel_per_s", ctypes.c_double)]
+                ("gvoxel_per_s", ctypes.c_double), ("cache_hits", _i64), ("cached", _i64)]
 
 
 PNM_REQ_QUEUED, PNM_REQ_RUNNING, PNM_REQ_DONE, PNM_REQ_FAILED, PNM_REQ_CANCELLED = range(5)

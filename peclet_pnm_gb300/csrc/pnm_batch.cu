@@ -605,6 +605,34 @@ Status batch_new(int device, int sm_count, cudaStream_t stream, void* pinned, in
 
 size_t batch_pinned_bytes(int nvol) { return 256 + (size_t)nvol * sizeof(VolResult); }
 
+Status batch_rebind(pnm_batch* b, cudaStream_t stream, const float* origin_xyz,
+                    const float* spacing_xyz, bool use_graph) {
+  if (b->pending) return Status{PNM_ERR_ARG, "a run is in flight"};
+  if (stream && !b->own_stream) b->stream = stream;
+  for (size_t i = 0; i < b->lay.vols.size(); ++i) {
+    VolDesc& v = b->lay.vols[i];
+    const float* o = origin_xyz + 3 * i;
+    const float* sp = spacing_xyz + 3 * i;
+    for (int a = 0; a < 3; ++a)
+      if (!(sp[a] > 0.0f) || !std::isfinite(sp[a]))
+        return Status{PNM_ERR_ARG, "spacing must be finite and positive"};
+    v.ox = o[0];
+    v.oy = o[1];
+    v.oz = o[2];
+    v.sx = sp[0];
+    v.sy = sp[1];
+    v.sz = sp[2];
+    v.thr = -1.5f * std::min(sp[0], std::min(sp[1], sp[2]));  // pore_extraction.hpp:163-164
+  }
+  PNM_CUDA(cudaSetDevice(b->device));
+  PNM_CUDA(cudaMemcpyAsync(const_cast<VolDesc*>(b->plan.vols), b->lay.vols.data(),
+                           b->lay.vols.size() * sizeof(VolDesc), cudaMemcpyHostToDevice,
+                           b->stream));
+  if (use_graph && !b->use_graph && b->graph_note.empty())
+    b->use_graph = true;  // captured on the next launch (unless a capture already failed)
+  return Status::ok();
+}
+
 }  // namespace pnm
 
 extern "C" {

@@ -206,6 +206,10 @@ Status batch_new(int device, int sm_count, cudaStream_t stream, void* pinned, in
                  const int32_t* dims_xyz, const float* origin_xyz, const float* spacing_xyz,
                  pnm_batch** out);
 size_t batch_pinned_bytes(int nvol);
+// Re-targets an idle batch: the stream its runs go to (batches on a borrowed stream only), the
+// origin and spacing of its volumes (same shapes), and graph replay from the next run on.
+Status batch_rebind(pnm_batch* b, cudaStream_t stream, const float* origin_xyz,
+                    const float* spacing_xyz, bool use_graph);
 }  // namespace pnm
 
 // The opaque handle of the C ABI.

@@ -1,7 +1,11 @@
 // Serving loop (pnm_server_*): a scheduler thread that admits queued extraction requests under a
 // device-memory budget, coalesces whatever is queued when a stream slot frees into one batch
 // (pnm_batch.cu), runs up to max_inflight batches concurrently on their own streams, and keeps
-// each request's results resident until the caller releases it.
+// each request's results resident until the caller releases it. A batch whose requests are all
+// released stays allocated in a small cache keyed by its volume shapes (counted against the
+// budget, evicted oldest first): a later group of the same shapes reuses it with new origins and
+// spacings instead of allocating again. Served batches enqueue their stages on every run: with
+// shapes that repeat only a few times, capturing a graph per shape costs more than it returns.
 //
 // Locking: `mu` guards the queue, the request table, the group lists and the statistics. The
 // scheduler never holds it across a CUDA call that can wait on a stream (batch creation, upload,
@@ -16,6 +20,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <list>
 #include <mutex>
 #include <new>
 #include <string>
@@ -34,6 +39,8 @@ constexpr int64_t kDefaultBudget = 120ll * 1000 * 1000 * 1000;  // 120 GB
 constexpr int kDefaultInflight = 3;
 constexpr int kDefaultBatchVolumes = 64;
 constexpr int64_t kDefaultBatchVoxels = 1ll << 28;
+constexpr int kCacheEntries = 96;   // idle batches kept for reuse
+constexpr int kPinBlocks = 512;     // pinned result blocks: running + held + cached batches
 
 struct Group;
 
@@ -53,6 +60,8 @@ struct Request {
 
 struct Group {
   pnm_batch* batch = nullptr;
+  void* pin = nullptr;              // this batch's pinned block (per-run figures)
+  std::vector<int32_t> dims;        // shapes (xyz per volume): the cache key
   std::vector<Request*> reqs;
   int slot = -1;
   int64_t bytes = 0;
@@ -61,13 +70,20 @@ struct Group {
   Clock::time_point t_launch;
   int live = 0;  // requests not yet released
   bool finished = false;
+  bool ok = false;
   struct pnm_server* srv = nullptr;
 };
 
 struct Slot {
   cudaStream_t stream = nullptr;
-  void* pinned = nullptr;
   bool busy = false;
+};
+
+struct Cached {
+  std::vector<int32_t> dims;
+  pnm_batch* batch;
+  void* pin;
+  int64_t bytes;
 };
 
 }  // namespace
@@ -83,6 +99,11 @@ struct pnm_server {
   std::deque<Request*> queue;
   std::unordered_map<int64_t, Request*> reqs;
   std::vector<Group*> running;
+  std::list<Cached> cache;          // idle batches, most recently used first
+  void* pin_arena = nullptr;        // pinned blocks for the batches' per-run figures
+  std::vector<void*> pin_free;
+  size_t pin_block = 0;
+  int64_t cache_hits = 0;
   int64_t next_id = 1;
   int64_t bytes_in_use = 0, peak_bytes = 0;
   int64_t submitted = 0, completed = 0, failed = 0, cancelled = 0, batches = 0;
@@ -110,10 +131,33 @@ int64_t plan_bytes(const std::vector<int32_t>& dims) {
   return b;
 }
 
-void destroy_group(pnm_server* s, Group* g) {  // called without mu; g is off every list
-  if (g->batch) pnm_batch_destroy(g->batch);
+// Frees a batch and returns its pinned block (caller holds mu; the CUDA calls do not block).
+void drop_batch(pnm_server* s, pnm_batch* b, void* pin) {
+  if (b) pnm_batch_destroy(b);
+  if (pin) s->pin_free.push_back(pin);
+}
+
+// Evicts the least recently used idle batch; false when the cache is empty (caller holds mu).
+bool evict_one(pnm_server* s) {
+  if (s->cache.empty()) return false;
+  Cached& c = s->cache.back();
+  s->bytes_in_use -= c.bytes;
+  drop_batch(s, c.batch, c.pin);
+  s->cache.pop_back();
+  return true;
+}
+
+// A group whose requests are all released: its batch goes to the cache when it ran cleanly
+// (caller holds mu).
+void retire_group(pnm_server* s, Group* g, bool ok) {
+  if (ok && g->batch) {
+    s->cache.push_front(Cached{g->dims, g->batch, g->pin, g->bytes});
+    while ((int)s->cache.size() > kCacheEntries) evict_one(s);
+  } else {
+    s->bytes_in_use -= g->bytes;
+    drop_batch(s, g->batch, g->pin);
+  }
   delete g;
-  (void)s;
 }
 
 // Completes a finished group: checks the run, records per-request figures and latencies.
@@ -148,6 +192,7 @@ void finish_group(pnm_server* s, Group* g, std::unique_lock<std::mutex>& lk) {
   if (rc != PNM_OK) s->last_error = err;
   s->t_last = std::max(s->t_last, t_done);
   g->finished = true;
+  g->ok = rc == PNM_OK;
   s->slots[g->slot].busy = false;
   s->running.erase(std::find(s->running.begin(), s->running.end(), g));
   s->cv_done.notify_all();
@@ -181,6 +226,9 @@ bool admit_one(pnm_server* s, std::unique_lock<std::mutex>& lk) {
     if (!take.empty() && voxels + r->voxels() > s->cfg.max_batch_voxels) break;
     dims.insert(dims.end(), r->dims, r->dims + 3);
     const int64_t b = plan_bytes(dims);
+    // idle cached batches give their memory back before anything waits for it
+    while (b >= 0 && s->bytes_in_use + b > s->cfg.budget_bytes && evict_one(s)) {
+    }
     if (b < 0 || s->bytes_in_use + b > s->cfg.budget_bytes) {
       dims.resize(dims.size() - 3);
       if (take.empty()) {
@@ -200,11 +248,37 @@ bool admit_one(pnm_server* s, std::unique_lock<std::mutex>& lk) {
     take.push_back(r);
     s->queue.pop_front();
   }
+  if (s->pin_free.empty()) {  // every pinned block is held: free idle batches first
+    while (s->pin_free.empty() && evict_one(s)) {
+    }
+    if (s->pin_free.empty()) {  // all held by results not yet released: retry later
+      for (auto it = take.rbegin(); it != take.rend(); ++it) s->queue.push_front(*it);
+      return false;
+    }
+  }
   auto* g = new Group();
   g->srv = s;
   g->slot = slot;
-  g->bytes = bytes;
+  g->dims = dims;
   g->reqs = take;
+  // an idle batch of exactly these shapes is reused (its memory is already counted)
+  pnm_batch* reuse = nullptr;
+  for (auto it = s->cache.begin(); it != s->cache.end(); ++it) {
+    if (it->dims == dims) {
+      reuse = it->batch;
+      g->pin = it->pin;
+      g->bytes = it->bytes;
+      s->cache.erase(it);
+      ++s->cache_hits;
+      break;
+    }
+  }
+  if (!reuse) {
+    g->pin = s->pin_free.back();
+    s->pin_free.pop_back();
+    g->bytes = bytes;
+    s->bytes_in_use += bytes;
+  }
   g->live = (int)take.size();
   for (size_t i = 0; i < take.size(); ++i) {
     take[i]->state = PNM_REQ_RUNNING;
@@ -212,7 +286,6 @@ bool admit_one(pnm_server* s, std::unique_lock<std::mutex>& lk) {
     take[i]->index = (int)i;
   }
   s->slots[slot].busy = true;
-  s->bytes_in_use += bytes;
   s->peak_bytes = std::max(s->peak_bytes, s->bytes_in_use);
   s->running.push_back(g);
   ++s->batches;
@@ -224,8 +297,11 @@ bool admit_one(pnm_server* s, std::unique_lock<std::mutex>& lk) {
     org.insert(org.end(), r->org, r->org + 3);
     spc.insert(spc.end(), r->spc, r->spc + 3);
   }
-  Status st = pnm::batch_new(s->device, s->sm_count, sl.stream, sl.pinned, PNM_BATCH_NO_GRAPH,
-                             (int)take.size(), dims.data(), org.data(), spc.data(), &g->batch);
+  Status st = reuse ? pnm::batch_rebind(reuse, sl.stream, org.data(), spc.data(), false)
+                    : pnm::batch_new(s->device, s->sm_count, sl.stream, g->pin,
+                                     PNM_BATCH_NO_GRAPH, (int)take.size(), dims.data(), org.data(),
+                                     spc.data(), &g->batch);
+  if (reuse) g->batch = reuse;
   int rc = st.code;
   std::string err = st.msg;
   for (size_t i = 0; rc == PNM_OK && i < take.size(); ++i)
@@ -241,14 +317,13 @@ bool admit_one(pnm_server* s, std::unique_lock<std::mutex>& lk) {
   if (rc != PNM_OK) {
     s->running.erase(std::find(s->running.begin(), s->running.end(), g));
     s->slots[slot].busy = false;
-    s->bytes_in_use -= bytes;
     fail_requests(s, take, rc);
     s->last_error = err;
     g->reqs.clear();
     lk.unlock();
     if (g->batch) cudaStreamSynchronize(sl.stream);
-    destroy_group(s, g);
     lk.lock();
+    retire_group(s, g, false);
   }
   return true;
 }
@@ -310,11 +385,13 @@ int pnm_server_create(pnm_ctx* ctx, const pnm_server_config* cfg, pnm_server** o
   bool ok = cudaSetDevice(s->device) == cudaSuccess &&
             cudaStreamCreateWithFlags(&s->io_stream, cudaStreamNonBlocking) == cudaSuccess;
   s->slots.resize(s->cfg.max_inflight);
-  for (Slot& sl : s->slots) {
+  for (Slot& sl : s->slots)
     ok = ok && cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) == cudaSuccess;
-    ok = ok && cudaMallocHost(&sl.pinned, pnm::batch_pinned_bytes(s->cfg.max_batch_volumes)) ==
-                   cudaSuccess;
-  }
+  s->pin_block = (pnm::batch_pinned_bytes(s->cfg.max_batch_volumes) + 255) & ~(size_t)255;
+  ok = ok && cudaMallocHost(&s->pin_arena, s->pin_block * kPinBlocks) == cudaSuccess;
+  if (ok)
+    for (int i = kPinBlocks - 1; i >= 0; --i)
+      s->pin_free.push_back(static_cast<char*>(s->pin_arena) + s->pin_block * i);
   if (!ok) {
     cudaGetLastError();
     ctx->c.last_error = "pnm_server_create: stream / pinned allocation failed";
@@ -346,14 +423,19 @@ void pnm_server_destroy(pnm_server* s) {
     if (g && std::find(groups.begin(), groups.end(), g) == groups.end()) groups.push_back(g);
     delete kv.second;
   }
-  for (Group* g : groups) destroy_group(s, g);
+  for (Group* g : groups) {
+    if (g->batch) pnm_batch_destroy(g->batch);
+    delete g;
+  }
+  for (Cached& c : s->cache) pnm_batch_destroy(c.batch);
+  s->cache.clear();
   for (Slot& sl : s->slots) {
     if (sl.stream) {
       cudaStreamSynchronize(sl.stream);
       cudaStreamDestroy(sl.stream);
     }
-    if (sl.pinned) cudaFreeHost(sl.pinned);
   }
+  if (s->pin_arena) cudaFreeHost(s->pin_arena);
   if (s->io_stream) cudaStreamDestroy(s->io_stream);
   delete s;
 }
@@ -484,7 +566,6 @@ int pnm_server_copy_out(pnm_server* s, int64_t ticket, pnm_pore* pores, int32_t*
 
 int pnm_server_release(pnm_server* s, int64_t ticket) {
   if (!s) return PNM_ERR_ARG;
-  Group* dead = nullptr;
   {
     std::lock_guard<std::mutex> lk(s->mu);
     Request* r = find(s, ticket);
@@ -494,13 +575,9 @@ int pnm_server_release(pnm_server* s, int64_t ticket) {
     Group* g = r->group;
     s->reqs.erase(ticket);
     delete r;
-    if (g && --g->live == 0 && g->finished) {
-      s->bytes_in_use -= g->bytes;
-      dead = g;
-    }
+    if (g && --g->live == 0 && g->finished) retire_group(s, g, g->ok);
     s->cv_sched.notify_all();  // memory may have freed up for queued requests
   }
-  if (dead) destroy_group(s, dead);
   return PNM_OK;
 }
 
@@ -532,6 +609,8 @@ int pnm_server_get_stats(pnm_server* s, pnm_server_stats* out) {
     out->mean_ms = sum / (double)v.size();
     out->max_ms = v.back();
   }
+  out->cache_hits = s->cache_hits;
+  out->cached = (int64_t)s->cache.size();
   if (s->have_first) {
     out->busy_s = std::chrono::duration<double>(s->t_last - s->t_first).count();
     if (out->busy_s > 0) out->gvoxel_per_s = (double)s->voxels_done / out->busy_s / 1e9;
@@ -542,7 +621,7 @@ int pnm_server_get_stats(pnm_server* s, pnm_server_stats* out) {
 int pnm_server_reset_stats(pnm_server* s) {
   if (!s) return PNM_ERR_ARG;
   std::lock_guard<std::mutex> lk(s->mu);
-  s->submitted = s->completed = s->failed = s->cancelled = s->batches = 0;
+  s->submitted = s->completed = s->failed = s->cancelled = s->batches = s->cache_hits = 0;
   s->voxels_done = 0;
   s->peak_bytes = s->bytes_in_use;
   s->lat_ms.clear();

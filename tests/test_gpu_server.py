@@ -47,7 +47,9 @@ def test_results_identical_alone_and_in_the_mix(gpu):
         for t, r in zip(tickets, reqs):
             _same(srv.result(t), pnm.extract_pore_network(*r, numpy=True), f"ticket {t}")
             srv.release(t)
-        assert srv.stats()["bytes_in_use"] == 0
+        st = srv.stats()  # only idle batches kept for reuse still hold memory
+        assert st["running"] == 0 and st["queued"] == 0
+        assert (st["bytes_in_use"] == 0) == (st["cached"] == 0)
 
 
 def test_device_resident_inputs(gpu):
@@ -98,3 +100,22 @@ def test_budget_refusal_cancel_and_recovery(gpu):
         st = srv.stats()
         assert st["peak_bytes"] <= budget
         assert st["cancelled"] == 1 and st["failed"] == 1
+
+
+def test_batch_reuse_keeps_results(gpu):
+    """Released batches are reused for later requests of the same shapes (new origin and spacing,
+    graph replay); every reused run still equals the request alone."""
+    pnm, _ = gpu
+    vols = _mix(3, seed=21)
+    with pnm.Server(max_inflight=1, max_batch_volumes=1) as srv:
+        for rep in range(3):
+            for i, (sdf, org, spc) in enumerate(vols):
+                spc2 = [spc[0] * (1.0 + 0.25 * rep), spc[1], spc[2] * (1.0 + 0.5 * rep)]
+                org2 = [org[0] + rep, org[1] - rep, org[2]]
+                t = srv.submit(sdf, org2, spc2)
+                assert srv.wait(t, 60.0) == PNM_OK
+                _same(srv.result(t), pnm.extract_pore_network(sdf, org2, spc2, numpy=True),
+                      f"rep {rep} volume {i}")
+                srv.release(t)
+        st = srv.stats()
+        assert st["cache_hits"] >= 6 and st["cached"] >= 1
