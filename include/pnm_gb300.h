@@ -145,6 +145,30 @@ int pnm_extract_pore_network_dev(pnm_ctx* ctx, const float* d_sdf, int32_t nx, i
 int pnm_segment_volume_dev(pnm_ctx* ctx, const float* d_sdf, int32_t nx, int32_t ny, int32_t nz,
                            const float spacing_xyz[3], int32_t* d_seg);
 
+/* Result of pnm_extract_network_flow_dev: the fields of pnm_flow_result as device arrays owned
+ * by the context. They are valid until the context's next call (or pnm_ctx_trim / destroy) and
+ * complete in stream order on the context's stream: work queued on that stream after the call
+ * may read them without a synchronisation; copy them out before the next call. */
+typedef struct {
+  int64_t n_pores, n_throats;
+  const pnm_pore* pores;
+  const double* pore_pressure;
+  const double* pore_residual;
+  const int32_t* throats; /* 2 * n_throats */
+  const double* throat_flow;
+  const double* throat_area;
+  const double* throat_dp;
+} pnm_flow_result_dev;
+
+/* extract_network_flow on device-resident inputs (SDF and float64 MAC fields, same layout as
+ * pnm_extract_network_flow): nothing crosses the host boundary but the counts. */
+int pnm_extract_network_flow_dev(pnm_ctx* ctx, const float* d_sdf, int32_t nx, int32_t ny,
+                                 int32_t nz, const float origin_xyz[3], const float spacing_xyz[3],
+                                 const double* d_u, const double* d_v, const double* d_w,
+                                 const double* d_p, const double* d_ox, const double* d_oy,
+                                 const double* d_oz, const double grad_p_xyz[3],
+                                 pnm_flow_result_dev* out);
+
 /* ---- allocation-free entry point -------------------------------------------------------------
  * No counterpart in the reference. extract_pores on a device SDF for callers that cannot let a
  * library allocate device memory: frameworks that hand out every byte of device memory from
@@ -297,6 +321,24 @@ int pnm_server_copy_out(pnm_server* s, int64_t ticket, pnm_pore* pores, int32_t*
 int pnm_server_release(pnm_server* s, int64_t ticket);
 int pnm_server_get_stats(pnm_server* s, pnm_server_stats* out);
 int pnm_server_reset_stats(pnm_server* s);
+
+/* ---- VTI ingest: SDFReader::read_vti (reference src/sdf_reader.cpp:28-152, bound as
+ * peclet.pnm.SDFReader.read_vti in src/pnm_bindings.cpp:87-102). ImageData with one appended raw
+ * float32 array behind a UInt64 byte count (the layout scripts/vti.py writes). The header is the
+ * first 8 KiB of text: resolution from WholeExtent (max - min + 1 per axis), the first Origin and
+ * Spacing attributes (0 when absent), the array after the first '_' past
+ * <AppendedData encoding="raw">. A byte count other than nx*ny*nz*4 reads what both allow and
+ * leaves the rest zero. These calls report failures through pnm_vti_last_error() (per thread);
+ * pnm_read_vti_dev also through pnm_last_error(ctx). */
+const char* pnm_vti_last_error(void);
+/* Parses the header: dims / origin / spacing as xyz, *data_bytes the file's byte count. */
+int pnm_read_vti_header(const char* path, int32_t dims_xyz[3], float origin_xyz[3],
+                        float spacing_xyz[3], int64_t* data_bytes);
+/* Reads the n = nx*ny*nz values (x fastest) into host memory. */
+int pnm_read_vti(const char* path, float* values, int64_t n);
+/* Streams the n values into device memory through pinned double-buffered staging on the
+ * context's stream (file reads overlap the copies); returns once they are on the device. */
+int pnm_read_vti_dev(pnm_ctx* ctx, const char* path, float* d_values, int64_t n);
 
 #ifdef __cplusplus
 }

@@ -21,5 +21,8 @@ FLAGS=(-std=c++20 -O2 -fPIC -shared -ffp-contract=off -I"$HERE/kokkos_compat" -I
 "$CXX" "${FLAGS[@]}" "$HERE/ref_capi.cpp" -o "$HERE/_ref/libpnm_ref.so" &
 # OpenMP: the same source on all host threads (timing only)
 "$CXX" "${FLAGS[@]}" -fopenmp -DPNM_SHIM_OPENMP "$HERE/ref_capi.cpp" -o "$HERE/_ref/libpnm_ref_omp.so" &
+# the reference's VTI reader (src/sdf_reader.cpp), pins pnm_read_vti
+"$CXX" -std=c++17 -O2 -fPIC -shared -I"$REF/src" "$HERE/ref_vti.cpp" "$REF/src/sdf_reader.cpp" \
+  -o "$HERE/_ref/libpnm_ref_vti.so" &
 wait
-echo "build_ref: built $HERE/_ref/libpnm_ref.so and libpnm_ref_omp.so"
+echo "build_ref: built $HERE/_ref/libpnm_ref.so, libpnm_ref_omp.so and libpnm_ref_vti.so"

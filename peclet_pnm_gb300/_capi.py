@@ -40,6 +40,12 @@ class PnmPore(ctypes.Structure):
                 ("radius", ctypes.c_float)]
 
 
+class PnmFlowResultDev(ctypes.Structure):
+    _fields_ = [("n_pores", _i64), ("n_throats", _i64), ("pores", _vp), ("pore_pressure", _vp),
+                ("pore_residual", _vp), ("throats", _vp), ("throat_flow", _vp),
+                ("throat_area", _vp), ("throat_dp", _vp)]
+
+
 class PnmFlowResult(ctypes.Structure):
     _fields_ = [("n_pores", _i64), ("n_throats", _i64), ("pores", _P(PnmPore)),
                 ("pore_pressure", _P(ctypes.c_double)), ("pore_residual", _P(ctypes.c_double)),
@@ -87,6 +93,9 @@ pnm_extract_network_flow = _sig("pnm_extract_network_flow", ctypes.c_int, _vp, _
                                 _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                 _P(_P(PnmFlowResult)))
 pnm_flow_result_free = _sig("pnm_flow_result_free", None, _P(PnmFlowResult))
+pnm_extract_network_flow_dev = _sig("pnm_extract_network_flow_dev", ctypes.c_int, _vp, _vp, _i32,
+                                    _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                    _P(PnmFlowResultDev))
 pnm_extract_pores_noalloc = _sig("pnm_extract_pores_noalloc", ctypes.c_int, _vp, _i32, _i32, _i32,
                                  _vp, _vp, _vp, _i64, _P(_i64), _vp)
 
@@ -163,6 +172,12 @@ pnm_server_release = _sig("pnm_server_release", ctypes.c_int, _vp, _i64)
 pnm_server_get_stats = _sig("pnm_server_get_stats", ctypes.c_int, _vp, _P(PnmServerStats))
 pnm_server_reset_stats = _sig("pnm_server_reset_stats", ctypes.c_int, _vp)
 
+pnm_vti_last_error = _sig("pnm_vti_last_error", ctypes.c_char_p)
+pnm_read_vti_header = _sig("pnm_read_vti_header", ctypes.c_int, ctypes.c_char_p, _vp, _vp, _vp,
+                           _P(_i64))
+pnm_read_vti = _sig("pnm_read_vti", ctypes.c_int, ctypes.c_char_p, _vp, _i64)
+pnm_read_vti_dev = _sig("pnm_read_vti_dev", ctypes.c_int, _vp, ctypes.c_char_p, _vp, _i64)
+
 #: every symbol include/pnm_gb300.h declares
 EXPORTED = ["pnm_ctx_create", "pnm_ctx_destroy", "pnm_last_error", "pnm_ctx_set_stream",
             "pnm_ctx_trim", "pnm_execution_space", "pnm_free", "pnm_extract_pores",
@@ -177,7 +192,9 @@ EXPORTED = ["pnm_ctx_create", "pnm_ctx_destroy", "pnm_last_error", "pnm_ctx_set_
             "pnm_batch_autotune", "pnm_server_create", "pnm_server_destroy",
             "pnm_server_last_error", "pnm_server_submit", "pnm_server_state", "pnm_server_wait",
             "pnm_server_cancel", "pnm_server_result", "pnm_server_copy_out", "pnm_server_release",
-            "pnm_server_get_stats", "pnm_server_reset_stats"]
+            "pnm_server_get_stats", "pnm_server_reset_stats", "pnm_vti_last_error",
+            "pnm_read_vti_header", "pnm_read_vti", "pnm_read_vti_dev",
+            "pnm_extract_network_flow_dev"]
 
 
 class PnmError(RuntimeError):
@@ -197,6 +214,7 @@ class Context:
                                 PNM_ERR_CUDA: "CUDA initialisation failed"}.get(
                 rc, f"pnm_ctx_create failed ({rc})"))
         self.h = h
+        self.device = int(device) if device >= 0 else None  # None: the device current at creation
 
     def check(self, rc: int):
         if rc != PNM_OK:

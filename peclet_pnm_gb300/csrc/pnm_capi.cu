@@ -494,8 +494,10 @@ int pnm_extract_network_flow(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t
     if (xfer.extra_done) PNM_CUDA(cudaStreamWaitEvent(c.stream, xfer.extra_done, 0));
     pnm::FlowInputs in{df[0], df[1], df[2], df[3], df[4], df[5], df[6],
                        {grad_p_xyz[0], grad_p_xyz[1], grad_p_xyz[2]}};
+    pnm::FlowOutputsDev od;
+    PNM_TRY(pnm::run_network_flow(c, st, origin_xyz, spacing_xyz, in, &od));
     pnm::FlowOutputsHost o;
-    PNM_TRY(pnm::run_network_flow(c, st, origin_xyz, spacing_xyz, in, &o));
+    PNM_TRY(pnm::flow_outputs_to_host(c, od, &o));
     record(c, st, 0, 0);
     auto* r = static_cast<pnm_flow_result*>(std::calloc(1, sizeof(pnm_flow_result)));
     if (!r) return Status{PNM_ERR_INTERNAL, "out of host memory"};
@@ -509,6 +511,47 @@ int pnm_extract_network_flow(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t
     r->throat_area = host_dup(o.throat_area.data(), o.throat_area.size());
     r->throat_dp = host_dup(o.throat_dp.data(), o.throat_dp.size());
     *out = r;
+    return Status::ok();
+  };
+  return finish(ctx, run());
+}
+
+int pnm_extract_network_flow_dev(pnm_ctx* ctx, const float* d_sdf, int32_t nx, int32_t ny,
+                                 int32_t nz, const float origin_xyz[3], const float spacing_xyz[3],
+                                 const double* d_u, const double* d_v, const double* d_w,
+                                 const double* d_p, const double* d_ox, const double* d_oy,
+                                 const double* d_oz, const double grad_p_xyz[3],
+                                 pnm_flow_result_dev* out) {
+  if (!ctx) return PNM_ERR_ARG;
+  Ctx& c = ctx->c;
+  auto run = [&]() -> Status {
+    if (!d_sdf || !origin_xyz || !d_u || !d_v || !d_w || !d_p || !grad_p_xyz || !out)
+      return Status{PNM_ERR_ARG, "null argument"};
+    *out = pnm_flow_result_dev{};
+    if ((d_ox == nullptr) != (d_oy == nullptr) || (d_ox == nullptr) != (d_oz == nullptr))
+      return Status{PNM_ERR_ARG, "pass all three openness arrays (ox,oy,oz) or none"};
+    const Dims d{nx, ny, nz};
+    PNM_TRY(pnm::check_dims(d, spacing_xyz, true));
+    if (d.n() == 0) return Status::ok();
+    if (3 * d.n() > (long long)INT_MAX - 8)
+      return Status{PNM_ERR_SHAPE, "volume too large for network flow: 3*nx*ny*nz must be < 2^31"};
+    PNM_TRY(enter(c));
+    pnm::SegState st;
+    PNM_TRY(pnm::run_segmentation(c, d_sdf, d, spacing_xyz, &st, /*all_ascent=*/true));
+    pnm::FlowInputs in{d_u, d_v, d_w, d_p, d_ox, d_oy, d_oz,
+                       {grad_p_xyz[0], grad_p_xyz[1], grad_p_xyz[2]}};
+    pnm::FlowOutputsDev od;
+    PNM_TRY(pnm::run_network_flow(c, st, origin_xyz, spacing_xyz, in, &od));
+    record(c, st, 0, 0);
+    out->n_pores = od.np;
+    out->n_throats = od.nt;
+    out->pores = od.pores;
+    out->pore_pressure = od.pore_pressure;
+    out->pore_residual = od.pore_residual;
+    out->throats = od.throats;
+    out->throat_flow = od.throat_flow;
+    out->throat_area = od.throat_area;
+    out->throat_dp = od.throat_dp;
     return Status::ok();
   };
   return finish(ctx, run());

@@ -192,8 +192,19 @@ struct FlowOutputsHost {
   std::vector<double> pore_pressure, pore_residual, throat_flow, throat_area, throat_dp;
   std::vector<int32_t> throats;
 };
+// Device-resident results of run_network_flow: context slots, valid until the context's next
+// call; complete once the context's stream reaches the point where run_network_flow returned.
+struct FlowOutputsDev {
+  long long np = 0, nt = 0;
+  pnm_pore* pores = nullptr;
+  double *pore_pressure = nullptr, *pore_residual = nullptr;
+  int32_t* throats = nullptr;
+  double *throat_flow = nullptr, *throat_area = nullptr, *throat_dp = nullptr;
+};
 Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const float spacing[3],
-                        const FlowInputs& in, FlowOutputsHost* out);
+                        const FlowInputs& in, FlowOutputsDev* out);
+// Copies the results to host vectors (synchronises the context's stream).
+Status flow_outputs_to_host(Ctx& c, const FlowOutputsDev& o, FlowOutputsHost* out);
 
 }  // namespace pnm
 

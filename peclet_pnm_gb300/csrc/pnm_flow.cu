@@ -682,12 +682,12 @@ inline int fixed_scale(double bound) {
 }  // namespace
 
 Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const float spacing[3],
-                        const FlowInputs& in, FlowOutputsHost* out) {
+                        const FlowInputs& in, FlowOutputsDev* out) {
   cudaStream_t s = c.stream;
   const Dims d = st.d;
   const long long n = d.n();
   const int np = st.n_pore_labels;
-  *out = FlowOutputsHost{};
+  *out = FlowOutputsDev{};
   if (np <= 0) return Status::ok();  // no pore label: empty network (:523-524)
 
   // seg (labels) for the flow-basin lookup
@@ -880,6 +880,22 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
   }
   PNM_CUDA(cudaGetLastError());
 
+  out->np = np;
+  out->nt = nt;
+  out->pores = pores;
+  out->pore_pressure = ppres;
+  out->pore_residual = resid;
+  out->throats = throats_d;
+  out->throat_flow = Q;
+  out->throat_area = A;
+  out->throat_dp = dp;
+  return Status::ok();
+}
+
+Status flow_outputs_to_host(Ctx& c, const FlowOutputsDev& o, FlowOutputsHost* out) {
+  cudaStream_t s = c.stream;
+  const long long np = o.np, nt = o.nt;
+  *out = FlowOutputsHost{};
   out->pores.resize(np);
   out->pore_pressure.resize(np);
   out->pore_residual.resize(np);
@@ -887,14 +903,21 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
   out->throat_flow.resize(nt);
   out->throat_area.resize(nt);
   out->throat_dp.resize(nt);
-  PNM_CUDA(cudaMemcpyAsync(out->pores.data(), pores, np * sizeof(pnm_pore), cudaMemcpyDeviceToHost, s));
-  PNM_CUDA(cudaMemcpyAsync(out->pore_pressure.data(), ppres, np * 8, cudaMemcpyDeviceToHost, s));
-  PNM_CUDA(cudaMemcpyAsync(out->pore_residual.data(), resid, np * 8, cudaMemcpyDeviceToHost, s));
+  if (np > 0) {
+    PNM_CUDA(cudaMemcpyAsync(out->pores.data(), o.pores, np * sizeof(pnm_pore),
+                             cudaMemcpyDeviceToHost, s));
+    PNM_CUDA(cudaMemcpyAsync(out->pore_pressure.data(), o.pore_pressure, np * 8,
+                             cudaMemcpyDeviceToHost, s));
+    PNM_CUDA(cudaMemcpyAsync(out->pore_residual.data(), o.pore_residual, np * 8,
+                             cudaMemcpyDeviceToHost, s));
+  }
   if (nt > 0) {
-    PNM_CUDA(cudaMemcpyAsync(out->throats.data(), throats_d, 2 * nt * 4, cudaMemcpyDeviceToHost, s));
-    PNM_CUDA(cudaMemcpyAsync(out->throat_flow.data(), Q, nt * 8, cudaMemcpyDeviceToHost, s));
-    PNM_CUDA(cudaMemcpyAsync(out->throat_area.data(), A, nt * 8, cudaMemcpyDeviceToHost, s));
-    PNM_CUDA(cudaMemcpyAsync(out->throat_dp.data(), dp, nt * 8, cudaMemcpyDeviceToHost, s));
+    PNM_CUDA(cudaMemcpyAsync(out->throats.data(), o.throats, 2 * nt * 4, cudaMemcpyDeviceToHost, s));
+    PNM_CUDA(cudaMemcpyAsync(out->throat_flow.data(), o.throat_flow, nt * 8, cudaMemcpyDeviceToHost,
+                             s));
+    PNM_CUDA(cudaMemcpyAsync(out->throat_area.data(), o.throat_area, nt * 8, cudaMemcpyDeviceToHost,
+                             s));
+    PNM_CUDA(cudaMemcpyAsync(out->throat_dp.data(), o.throat_dp, nt * 8, cudaMemcpyDeviceToHost, s));
   }
   PNM_CUDA(cudaStreamSynchronize(s));
   return Status::ok();
