@@ -169,6 +169,29 @@ int pnm_extract_network_flow_dev(pnm_ctx* ctx, const float* d_sdf, int32_t nx, i
                                  const double* d_oz, const double grad_p_xyz[3],
                                  pnm_flow_result_dev* out);
 
+/* ---- pore-network post-processing (scripts/demo_network_flow_packing.py:44-67) --------------
+ * Throat conductance g = Q / dp (IEEE division: dp = 0 gives +-inf or NaN) and the statistics
+ * the reference's demo derives from an extract_network_flow result. Means are over throats,
+ * maxima of absolute values propagate NaN (as numpy's max); sums are folded in a fixed order
+ * (deterministic on a given device). mass_balance_ok = max|pore_residual| < 1e-6 * max|throat_flow| and every g
+ * finite (the demo's PASS test; 1 for an empty network). */
+typedef struct {
+  int64_t n_pores, n_throats;
+  double mean_abs_flow, max_abs_flow, mean_abs_dp, max_abs_residual;
+  int64_t n_positive_conductance; /* throats with g > 0 */
+  int64_t n_finite_conductance;
+  double mean_coordination;       /* 2 * n_throats / n_pores (repeated pairs count) */
+  int32_t max_coordination;
+  int32_t mass_balance_ok;
+} pnm_flow_stats;
+
+/* Statistics of device-resident flow results (any device arrays in the pnm_flow_result_dev
+ * layout, e.g. straight from pnm_extract_network_flow_dev; throats 8-byte aligned). Optional
+ * outputs: d_conductance (n_throats doubles) and d_coordination (n_pores int32, throats per pore
+ * label). Runs on the context's stream and returns when the statistics are on the host. */
+int pnm_flow_stats_dev(pnm_ctx* ctx, const pnm_flow_result_dev* r, double* d_conductance,
+                       int32_t* d_coordination, pnm_flow_stats* out);
+
 /* ---- allocation-free entry point -------------------------------------------------------------
  * No counterpart in the reference. extract_pores on a device SDF for callers that cannot let a
  * library allocate device memory: frameworks that hand out every byte of device memory from

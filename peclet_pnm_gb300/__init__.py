@@ -14,7 +14,8 @@ Same Python surface as the reference module (``src/pnm_bindings.cpp:86-209``, re
 * ``SDFReader.read_vti(filename) -> (sdf_3d, origin_zyx, spacing_zyx)`` (``vti.py``)
 
 Beyond the reference: ``*_device`` calls on CUDA tensors / DLPack arrays (``device.py``), batches
-(``batch.py``), a serving loop (``server.py``) and ``read_vti_device``.
+(``batch.py``), a serving loop (``server.py``), ``read_vti_device`` and ``network_stats``
+(conductance and network statistics of a flow result, ``post.py``).
 
 Arrays are ``(Nz, Ny, Nx)`` C-order (x fastest); the SDF is cast to float32 and the MAC fields
 to float64 like nanobind's implicit conversion; origin / spacing are zyx and cast to float32.
@@ -33,7 +34,8 @@ __all__ = ["Pore", "extract_pores", "segment_volume", "extract_topology_gpu",
            "extract_pore_network", "extract_network_flow", "execution_space", "Context",
            "PnmError", "Batch", "extract_pore_network_batch", "batch_plan_bytes", "Server",
            "SDFReader", "read_vti_device", "save_vti", "write_sdf_vti", "write_edge_list",
-           "segment_volume_device", "extract_pore_network_device", "extract_network_flow_device"]
+           "segment_volume_device", "extract_pore_network_device", "extract_network_flow_device",
+           "network_stats", "throat_conductance"]
 
 execution_space = _capi.pnm_execution_space().decode()
 
@@ -42,6 +44,7 @@ from .server import Server  # noqa: E402
 from .vti import SDFReader, read_vti_device, save_vti, write_edge_list, write_sdf_vti  # noqa: E402
 from .device import (extract_network_flow_device, extract_pore_network_device,  # noqa: E402
                      segment_volume_device)
+from .post import network_stats, throat_conductance  # noqa: E402
 
 
 class Pore:

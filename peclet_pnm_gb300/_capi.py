@@ -46,6 +46,14 @@ class PnmFlowResultDev(ctypes.Structure):
                 ("throat_area", _vp), ("throat_dp", _vp)]
 
 
+class PnmFlowStats(ctypes.Structure):
+    _fields_ = [("n_pores", _i64), ("n_throats", _i64), ("mean_abs_flow", ctypes.c_double),
+                ("max_abs_flow", ctypes.c_double), ("mean_abs_dp", ctypes.c_double),
+                ("max_abs_residual", ctypes.c_double), ("n_positive_conductance", _i64),
+                ("n_finite_conductance", _i64), ("mean_coordination", ctypes.c_double),
+                ("max_coordination", _i32), ("mass_balance_ok", _i32)]
+
+
 class PnmFlowResult(ctypes.Structure):
     _fields_ = [("n_pores", _i64), ("n_throats", _i64), ("pores", _P(PnmPore)),
                 ("pore_pressure", _P(ctypes.c_double)), ("pore_residual", _P(ctypes.c_double)),
@@ -96,6 +104,8 @@ pnm_flow_result_free = _sig("pnm_flow_result_free", None, _P(PnmFlowResult))
 pnm_extract_network_flow_dev = _sig("pnm_extract_network_flow_dev", ctypes.c_int, _vp, _vp, _i32,
                                     _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                     _P(PnmFlowResultDev))
+pnm_flow_stats_dev = _sig("pnm_flow_stats_dev", ctypes.c_int, _vp, _P(PnmFlowResultDev), _vp, _vp,
+                          _P(PnmFlowStats))
 pnm_extract_pores_noalloc = _sig("pnm_extract_pores_noalloc", ctypes.c_int, _vp, _i32, _i32, _i32,
                                  _vp, _vp, _vp, _i64, _P(_i64), _vp)
 
@@ -194,7 +204,7 @@ EXPORTED = ["pnm_ctx_create", "pnm_ctx_destroy", "pnm_last_error", "pnm_ctx_set_
             "pnm_server_cancel", "pnm_server_result", "pnm_server_copy_out", "pnm_server_release",
             "pnm_server_get_stats", "pnm_server_reset_stats", "pnm_vti_last_error",
             "pnm_read_vti_header", "pnm_read_vti", "pnm_read_vti_dev",
-            "pnm_extract_network_flow_dev"]
+            "pnm_extract_network_flow_dev", "pnm_flow_stats_dev"]
 
 
 class PnmError(RuntimeError):

@@ -20,7 +20,7 @@ INCLUDE = os.path.join(ROOT, "include")
 OBJDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpnm_gb300.so")
 SOURCES = ["pnm_segment.cu", "pnm_flow.cu", "pnm_capi.cu", "pnm_noalloc.cu", "pnm_batch.cu",
-           "pnm_server.cu", "pnm_vti.cu"]
+           "pnm_server.cu", "pnm_vti.cu", "pnm_post.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no floating-point contraction anywhere (float centroids and the float64

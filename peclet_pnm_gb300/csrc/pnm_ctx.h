@@ -68,6 +68,8 @@ enum Slot : int {
   S_FPAR, S_FFILM, S_FMINCORE, S_FLABEL, S_ROOTFLAG, S_SLOTOF, S_PEAK, S_NPORES_OUT,
   S_PPRES, S_REC, S_ACC, S_TDP, S_THROATS, S_MAXBITS, S_FLOWOUT, S_ULIST, S_EDGES, S_NXT, S_STEPS,
   S_COORD,
+  // post-processing
+  S_POST, S_POSTCOORD,
   S_COUNT
 };
 

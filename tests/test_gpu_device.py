@@ -4,6 +4,7 @@ C ABI) and of the streaming VTI reader (pnm_read_vti_dev).
 Device calls take torch CUDA tensors (or DLPack producers) and must give exactly what the
 host-pointer calls give on the same volume; those are pinned to the oracle elsewhere, and here
 segment_volume / extract_pore_network are checked against the oracle directly as well."""
+import math
 import os
 
 import numpy as np
@@ -182,3 +183,57 @@ def test_read_vti_device_then_extract(gpu, port, torch, tmp_path):
     assert np.array_equal(sorted_pores(pores.cpu().numpy()).view(np.int32),
                           sorted_pores(op).view(np.int32))
     assert np.array_equal(pairs.cpu().numpy(), np.asarray(opairs).reshape(-1, 2))
+
+
+# ---- post-processing on the device ------------------------------------------------------------
+@pytest.mark.parametrize("case", standard_cases()[:5], ids=lambda c: c[0])
+def test_network_stats_device_matches_host(gpu, torch, case):
+    """pnm_flow_stats_dev against the numpy arithmetic of the reference demo: conductance
+    bitwise (IEEE division on both sides), counts and maxima exact, means within 1e-12."""
+    pnm, _ = gpu
+    from peclet_pnm_gb300 import device
+
+    name, sdf, org, spc = case
+    f = flow_fields(sdf)
+    r = device.extract_network_flow_device(torch.from_numpy(sdf).cuda(), org, spc,
+                                           *[torch.from_numpy(x).cuda() for x in f[:4]])
+    hs = pnm.network_stats({k: v.cpu().numpy() for k, v in r.items()})
+    ds = pnm.network_stats(r)
+    assert ds["conductance"].is_cuda
+    assert np.array_equal(ds["conductance"].cpu().numpy().view(np.uint64),
+                          hs["conductance"].view(np.uint64))
+    assert np.array_equal(ds["coordination"].cpu().numpy(), hs["coordination"])
+    for k in ("n_pores", "n_throats", "max_abs_flow", "max_abs_residual", "max_coordination",
+              "frac_positive_conductance", "all_conductance_finite", "mass_balance_ok",
+              "mean_coordination"):
+        assert ds[k] == hs[k], (k, ds[k], hs[k])
+    for k in ("mean_abs_flow", "mean_abs_dp"):
+        assert abs(ds[k] - hs[k]) <= 1e-12 * abs(hs[k]), k
+
+
+def test_network_stats_device_special_values(gpu, torch):
+    pnm, _ = gpu
+    net = {"pore_residual": np.array([1e-12, -3e-12, np.nan, 2e-12]),
+           "throats": np.array([[1, 2], [1, 3], [2, 3], [2, 3], [3, 4]], np.int32),
+           "throat_flow": np.array([2.0, -1.0, 0.5, 0.0, 4.0]),
+           "throat_dp": np.array([1.0, 2.0, -0.5, 0.0, 0.0])}
+    hs = pnm.network_stats(net)
+    ds = pnm.network_stats({k: torch.from_numpy(v).cuda() for k, v in net.items()})
+    g = ds["conductance"].cpu().numpy()
+    assert np.array_equal(np.isnan(g), np.isnan(hs["conductance"]))
+    assert np.array_equal(g[~np.isnan(g)], hs["conductance"][~np.isnan(hs["conductance"])])
+    assert math.isnan(ds["max_abs_residual"]) and math.isnan(hs["max_abs_residual"])
+    for k in ("frac_positive_conductance", "all_conductance_finite", "mass_balance_ok",
+              "max_coordination", "max_abs_flow"):
+        assert ds[k] == hs[k], k
+    assert ds["coordination"].cpu().tolist() == [2, 3, 4, 1]
+    big = 300_000  # several blocks of partials
+    rng = np.random.default_rng(9)
+    net2 = {"pore_residual": rng.normal(0, 1e-9, 50_000),
+            "throats": rng.integers(1, 50_001, (big, 2)).astype(np.int32),
+            "throat_flow": rng.normal(0, 1, big), "throat_dp": rng.normal(0, 1, big)}
+    hs2 = pnm.network_stats(net2)
+    ds2 = pnm.network_stats({k: torch.from_numpy(v).cuda() for k, v in net2.items()})
+    assert np.array_equal(ds2["coordination"].cpu().numpy(), hs2["coordination"])
+    assert ds2["max_abs_flow"] == hs2["max_abs_flow"]
+    assert abs(ds2["mean_abs_flow"] - hs2["mean_abs_flow"]) <= 1e-12 * hs2["mean_abs_flow"]
