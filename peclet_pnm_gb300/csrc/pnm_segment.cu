@@ -27,31 +27,47 @@ constexpr int PLAIN_FLOOD_PER_SM = 4;  // persistent flood loop: resident blocks
 constexpr int kBig = INT_MAX;           // unset min-index / non-marker parent
 
 // ---- 1. SDF pass ---------------------------------------------------------------------------
-// A 32x8x8 tile in shared memory with a one-voxel periodic halo; one warp = one 32-voxel x-row
-// chunk, each thread walks the 8 z-planes of its column. Per voxel:
+// A 32x8xTZ tile in shared memory with a one-voxel periodic halo; one warp = one 32-voxel x-row
+// chunk, each thread walks the z-planes of its column. Per voxel:
 //  * ascent direction = lexicographic max of (sdf, wrapped index) over the voxel and its 26
-//    neighbours, scanned dz->dy->dx with the reference's comparisons (pore_extraction.hpp:284-304,
-//    :632-644); it points at the voxel itself exactly when the voxel is a strict local max
-//    (:93-104). Stored as direction bits of `code` and as the neighbour's id in nxt;
+//    neighbours (pore_extraction.hpp:284-304, :632-644); it points at the voxel itself exactly
+//    when the voxel is a strict local max (:93-104). Stored as direction bits of `code` and as
+//    the neighbour's id in nxt;
 //  * class (marker :177, flood :245-248, pore :276), flood seed (has a marker neighbour), peak
 //    bit for extract_pores (:89-106): !(sdf <= 0) and the voxel is its own ascent target.
+// The lexicographic maximum is taken separably: over x within each halo row, then over y, then
+// over z from a three-plane window in registers. The order is total on (value key, wrapped
+// index), so the separable maximum is the 27-point one, ties included. Value keys order the
+// floats as the reference's comparisons do: -0 == +0, and NaN below every number (a NaN
+// neighbour never wins; a NaN voxel stays on itself, as nothing compares above it).
 // Marker CCL (:181-230), first half: a marker's union-find parent is the first marker of its run
 // inside the 32-voxel chunk (runs are connected), and the chunk's marker bits go to the marker
 // bitmap (one word per chunk, bits past the volume's x extent clear) for k_ccl_words.
 
+__device__ __forceinline__ uint32_t ord_key(float v) {
+  const uint32_t b = __float_as_uint(v == 0.0f ? 0.0f : v);
+  return v != v ? 0u : (b ^ ((b >> 31) ? 0xffffffffu : 0x80000000u));
+}
+constexpr uint32_t kOrdZero = 0x80000000u;  // ord_key(+-0); 0 is NaN, nothing else maps there
+// (o1, p1) above (o0, p0) in (value key, position) order
+__device__ __forceinline__ bool key_above(uint32_t o1, uint32_t p1, uint32_t o0, uint32_t p0) {
+  return (((uint64_t)o1 << 32) | p1) > (((uint64_t)o0 << 32) | p0);
+}
+
 template <bool ALL_ASCENT, class G, int TZ = 8>
-__global__ void __launch_bounds__(TX* TY)
+__global__ void __launch_bounds__(TX* TY, 6)
     k_sdf_pass(const float* __restrict__ sdf, G geo, uint8_t* __restrict__ code,
                int* __restrict__ nxt, int* __restrict__ L, uint32_t* __restrict__ peakbits,
                uint32_t* __restrict__ mbits) {
   constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2, NT = TX * TY;
-  __shared__ float s[HZ][HY][HX];
+  __shared__ uint32_t so[HZ][HY][HX];     // value keys of the halo tile
   __shared__ int wx[HX], wy[HY], wz[HZ];
-  __shared__ unsigned rowm[HZ][HY];       // markers of each halo row at x = X0 .. X0+31
-  __shared__ unsigned char rowh[HZ][HY];  // bit 0: marker at x = X0-1; bit 1: at x = X0+32
+  __shared__ unsigned rowm[HZ][HY];  // markers of each halo row at x = X0 .. X0+31
+  __shared__ unsigned rowd[HZ][HY];  // the same row's markers at x-1, x or x+1 (x = X0 .. X0+31)
   const Box bx = geo.tile(blockIdx.x, TX, TY, TZ, false);
   const int off = bx.off;  // the volume's first global voxel id: added to every stored id
   const float thr = bx.thr;
+  const uint32_t othr = ord_key(thr);
   sdf += off;
   code += off;
   nxt += off;
@@ -74,17 +90,17 @@ __global__ void __launch_bounds__(TX* TY)
     const int hy = r % HY, hz = r / HY;
     const float* src = sdf + (wz[hz] * nxy + wy[hy] * nx);
     const float v0 = __ldg(&src[wx[lane + 1]]);
-    s[hz][hy][lane + 1] = v0;
+    so[hz][hy][lane + 1] = ord_key(v0);
     float vh = 0.0f;
     if (lane < 2) {
       vh = __ldg(&src[wx[lane == 0 ? 0 : HX - 1]]);
-      s[hz][hy][lane == 0 ? 0 : HX - 1] = vh;
+      so[hz][hy][lane == 0 ? 0 : HX - 1] = ord_key(vh);
     }
     const unsigned m = __ballot_sync(0xffffffffu, v0 < thr);
-    const unsigned h = __ballot_sync(0xffffffffu, lane < 2 && vh < thr);
+    const unsigned h = __ballot_sync(0xffffffffu, lane < 2 && vh < thr);  // x = X0-1, X0+32
     if (lane == 0) {
       rowm[hz][hy] = m;
-      rowh[hz][hy] = (unsigned char)(h & 3u);
+      rowd[hz][hy] = m | (m << 1) | (m >> 1) | (h & 1u) | ((h & 2u) << 30);
     }
   }
   __syncthreads();
@@ -92,67 +108,87 @@ __global__ void __launch_bounds__(TX* TY)
   const int gx = X0 + tx, gy = Y0 + ty;
   const bool inxy = gx < nx && gy < ny;
   const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
-  for (int tz = 0; tz < TZ; ++tz) {
+  // x positions of the three candidates of this lane and the y offsets of this warp's rows
+  const uint32_t px0 = wx[lane], px1 = wx[lane + 1], px2 = wx[lane + 2];
+  const uint32_t py[3] = {(uint32_t)(wy[ty] * nx), (uint32_t)(wy[ty + 1] * nx),
+                          (uint32_t)(wy[ty + 2] * nx)};
+  uint32_t wo[3] = {0, 0, 0}, wp[3] = {0, 0, 0};  // window: x-y maxima of the last three planes
+  int wd[3] = {0, 0, 0};
+#pragma unroll 1
+  for (int hz = 0; hz < HZ; ++hz) {
+    // maximum over the 3x3 (y, x) block of plane hz around this lane
+    uint32_t yo = 0, yp = 0;
+    int yd = 0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const uint32_t* row = &so[hz][ty + j][lane];
+      uint32_t o = row[0], q = px0;
+      int d = 0;
+      const uint32_t o1 = row[1], o2 = row[2];
+      if (key_above(o1, px1, o, q)) {
+        o = o1;
+        q = px1;
+        d = 1;
+      }
+      if (key_above(o2, px2, o, q)) {
+        o = o2;
+        q = px2;
+        d = 2;
+      }
+      q += py[j];
+      if (j == 0 || key_above(o, q, yo, yp)) {
+        yo = o;
+        yp = q;
+        yd = 3 * j + d;
+      }
+    }
+    wo[0] = wo[1];
+    wp[0] = wp[1];
+    wd[0] = wd[1];
+    wo[1] = wo[2];
+    wp[1] = wp[2];
+    wd[1] = wd[2];
+    wo[2] = yo;
+    wp[2] = yp + (uint32_t)(wz[hz] * nxy);
+    wd[2] = yd;
+    if (hz < 2) continue;
+    const int tz = hz - 2;  // output plane: its z-neighbours are the window's planes
     const int gz = Z0 + tz;
     const bool valid = inxy && gz < nz;
     const int ci = gz * nxy + gy * nx + gx;
+    const uint32_t oc = so[tz + 1][ty + 1][tx + 1];
+    const int cls = oc > kOrdZero ? CLS_PORE
+                    : (oc != 0u && oc < othr) ? CLS_MARKER
+                    : (oc == 0u || oc < kOrdZero) ? CLS_FLOOD
+                                                  : CLS_ZERO;
+    // flood seed: a marker among the 26 neighbours (the voxel itself is no marker)
+    unsigned nb = 0;
+    if (__any_sync(0xffffffffu, valid && cls == CLS_FLOOD)) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) nb |= rowd[tz + k / 3][ty + k % 3];
+    }
     if (valid) {
-      const float* c0 = &s[tz + 1][ty + 1][tx + 1];
-      const float cv = *c0;
-      const int cls = cv > 0.0f ? CLS_PORE
-                                : (cv < thr ? CLS_MARKER : (!(cv >= 0.0f) ? CLS_FLOOD : CLS_ZERO));
+      const bool up = oc > kOrdZero || oc == 0u;  // !(sdf <= 0): where walks start, peaks sit
       int bk = kSelf;
-      // ascent: every voxel for the flow basins, otherwise where a walk starts (sdf > 0) or a
-      // peak can sit (!(sdf <= 0), NaN included)
-      if (ALL_ASCENT || !(cv <= 0.0f)) {
-        float bv = cv;
-        bool tie = false;
-        // strict scan; any equality with the running maximum takes the exact tie-aware scan
-#pragma unroll
-        for (int k = 0; k < 27; ++k) {
-          if (k == kSelf) continue;
-          const float nv = c0[(k / 9 - 1) * (HY * HX) + ((k / 3) % 3 - 1) * HX + (k % 3 - 1)];
-          tie |= (nv == bv);
-          if (nv > bv) {
-            bv = nv;
-            bk = k;
-          }
+      if (ALL_ASCENT || up) {
+        uint32_t bo = wo[0], bp = wp[0];
+        int bd = wd[0];
+        if (key_above(wo[1], wp[1], bo, bp)) {
+          bo = wo[1];
+          bp = wp[1];
+          bd = 9 + wd[1];
         }
-        if (tie) {
-          bv = cv;
-          bk = kSelf;
-          int bi = ci;
-#pragma unroll 1
-          for (int k = 0; k < 27; ++k) {
-            if (k == kSelf) continue;
-            const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
-            const float nv = s[tz + 1 + dz][ty + 1 + dy][tx + 1 + dx];
-            const int ni = wz[tz + 1 + dz] * nxy + wy[ty + 1 + dy] * nx + wx[tx + 1 + dx];
-            if (nv > bv) {
-              bv = nv;
-              bk = k;
-              bi = ni;
-            } else if (nv == bv && ni > bi) {  // tie: the larger wrapped index wins
-              bk = k;
-              bi = ni;
-            }
-          }
+        if (key_above(wo[2], wp[2], bo, bp)) {
+          bo = wo[2];
+          bp = wp[2];
+          bd = 18 + wd[2];
         }
-        nxt[ci] = off + (bk == kSelf ? ci
-                                     : wz[tz + bk / 9] * nxy + wy[ty + (bk / 3) % 3] * nx +
-                                           wx[tx + bk % 3]);
-        if (!(cv <= 0.0f) && bk == kSelf) atomicOr(&peakbits[ci >> 5], 1u << (ci & 31));
+        // the voxel itself (or a wrapped copy of it) wins, and a NaN voxel stays
+        bk = ((int)bp == ci || oc == 0u) ? kSelf : bd;
+        nxt[ci] = off + (bk == kSelf ? ci : (int)bp);
+        if (up && bk == kSelf) atomicOr(&peakbits[ci >> 5], 1u << (ci & 31));
       }
-      bool seed = false;  // a shallow-solid voxel with a marker neighbour (NaN is never < thr)
-      if (cls == CLS_FLOOD) {
-        float vmin = c0[-(HY * HX) - HX - 1];
-#pragma unroll
-        for (int k = 1; k < 27; ++k) {
-          if (k == kSelf) continue;
-          vmin = fminf(vmin, c0[(k / 9 - 1) * (HY * HX) + ((k / 3) % 3 - 1) * HX + (k % 3 - 1)]);
-        }
-        seed = vmin < thr;
-      }
+      const bool seed = cls == CLS_FLOOD && ((nb >> lane) & 1u);
       code[ci] = make_code(bk, cls, seed);
     }
     // marker runs of this chunk row
