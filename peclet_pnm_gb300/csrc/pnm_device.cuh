@@ -47,14 +47,27 @@ __device__ __forceinline__ void st_relaxed(int* p, int v) {
   asm volatile("st.relaxed.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// A read through L1 that may return an older value of the word (another SM's later store is not
+// seen until the line leaves this SM's L1). Used for union-find parents, which only ever move to
+// smaller ids of the same set: an older parent is still an ancestor, so a find over such reads
+// still ends in the set, and every link re-checks with an atomic that sees the current value.
+// Hot words (the roots of big components) are then served by L1 instead of one L2 slice.
+__device__ __forceinline__ int ld_cached(const int* p) {
+  int v;
+  asm volatile("ld.global.ca.s32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+
 // Bounded find with path halving (ECL-CC style). Parents always point to smaller ids in the same
 // set, so a concurrent atomicMin link can only shorten a path; halving stores never break a set.
+// It may end on a node that was linked meanwhile (see ld_cached): callers that link re-check
+// with the atomic, and after the linking kernel every node's chain ends at the root.
 constexpr int kUfLimit = 1 << 22;
 __device__ __forceinline__ int uf_find(int* L, int x, unsigned* err) {
   for (int it = 0; it < kUfLimit; ++it) {
-    const int p = ld_relaxed(&L[x]);
+    const int p = ld_cached(&L[x]);
     if (p == x) return x;
-    const int gp = ld_relaxed(&L[p]);
+    const int gp = ld_cached(&L[p]);
     if (gp != p) st_relaxed(&L[x], gp);
     x = gp;
   }
