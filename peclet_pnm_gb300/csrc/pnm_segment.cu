@@ -379,9 +379,10 @@ __global__ void __launch_bounds__(RTX* RTY)
     }
     if (valid) key[v] = k;
     // first-appearance minimum for pore basins: the first lane of each run of lanes with the same
-    // root carries that run's minimum voxel id
+    // root carries that run's minimum voxel id. L[root] of a pore root only decreases, so a read
+    // (possibly older, see ld_cached) at or below v shows the atomic would change nothing.
     const int pa = __shfl_up_sync(0xffffffffu, agg, 1);
-    if (agg >= 0 && (lane == 0 || pa != agg)) {
+    if (agg >= 0 && (lane == 0 || pa != agg) && ld_cached(&L[agg]) > v) {
       const int old = atomicMin(&L[agg], v);
       if (old == kBig) new_key = true;
     }
@@ -668,11 +669,19 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
   return x;
 }
 constexpr int kMaxProbe = 4096;
+// A slot changes once, from kEmpty to its final key, so a read through L1 that returns an older
+// value returns kEmpty (and the CAS decides) or that final key; repeated proposals of a popular
+// pair are then answered by L1.
+__device__ __forceinline__ unsigned long long ld_slot(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.global.ca.u64 %0, [%1];" : "=l"(v) : "l"(p));
+  return v;
+}
 __device__ __forceinline__ void hash_insert(unsigned long long* table, uint64_t mask, uint64_t k,
                                             unsigned* err, unsigned* count) {
   uint64_t h = mix64(k) & mask;
   for (int p = 0; p < kMaxProbe; ++p) {
-    const unsigned long long cur = *((volatile unsigned long long*)&table[h]);
+    const unsigned long long cur = ld_slot(&table[h]);
     if (cur == k) return;
     if (cur == kEmpty) {
       const unsigned long long old = atomicCAS(&table[h], kEmpty, (unsigned long long)k);
@@ -690,11 +699,16 @@ __device__ __forceinline__ void hash_insert(unsigned long long* table, uint64_t 
 // Label of voxel v for a warp whose lanes hold consecutive voxels of one row: from key[] and
 // the id table in L[] — lanes repeating the previous lane's key take the label from the first
 // lane of their run instead of gathering it again — or straight from a seg array.
+// Labels come as ids (key[] entries, or seg[] labels themselves) and the labels they map to:
+// distinct keys have distinct labels (pore roots, marker roots, none), so faces compare ids and
+// only differing faces look their labels up. The seg output needs every label: a warp's row of
+// ids is mapped with one lookup per run of lanes holding the same id.
 struct KeyLabels {
   const int* key;
   const int* L;
-  __device__ int operator()(int v, bool active) const {
-    const int k = active ? __ldg(&key[v]) : KEY_NONE;
+  __device__ int id(int v, bool active) const { return active ? __ldg(&key[v]) : KEY_NONE; }
+  __device__ int label(int k) const { return label_of_key(L, k); }
+  __device__ int labels_warp(int k, bool active) const {
     const unsigned lane = threadIdx.x & 31;
     const int pk = __shfl_up_sync(0xffffffffu, k, 1);
     const bool lead = lane == 0 || pk != k;
@@ -709,21 +723,18 @@ struct KeyLabels {
 };
 struct SegLabels {
   const int* seg;
-  __device__ int operator()(int v, bool active) const { return active ? __ldg(&seg[v]) : 0; }
+  __device__ int id(int v, bool active) const { return active ? __ldg(&seg[v]) : 0; }
+  __device__ int label(int k) const { return k; }
+  __device__ int labels_warp(int k, bool) const { return k; }
   __device__ SegLabels at(int off) const { return SegLabels{seg + off}; }
 };
 
 // One pass over 32 x 8 x 16 bricks (a warp owns a 32-voxel x-row and walks 16 z-planes): seg[v]
-// (optional) and every differing (+x,+y,+z) periodic face pair into the hash set. The +x label
-// comes from the neighbouring lane, the +z label is carried to the next plane. Lanes proposing
-// the pair of the previous lane skip their insert; lab_min/lab_max track the label range. In a
+// (optional) and every differing (+x,+y,+z) periodic face pair into the hash set. The +x id
+// comes from the neighbouring lane, the +z id is carried to the next plane. Lanes proposing the
+// pair of the previous lane skip their insert; lab_min/lab_max track the label range. In a
 // batch, pair labels are ordered as gbase(volume) + label, so one set holds every volume's pairs
 // and sorting it groups them by volume.
-__device__ __forceinline__ int lab_one(const KeyLabels& l, int v) {
-  return label_of_key(l.L, __ldg(&l.key[v]));
-}
-__device__ __forceinline__ int lab_one(const SegLabels& l, int v) { return __ldg(&l.seg[v]); }
-
 constexpr int STX = 32, STY = 8, STZ = 16;
 template <class G, class Lab>
 __global__ void __launch_bounds__(STX* STY)
@@ -744,24 +755,25 @@ __global__ void __launch_bounds__(STX* STY)
   const int nxy = nx * ny;
   int lmin = INT_MAX, lmax = INT_MIN;
   if (y >= ny) return;  // warp-uniform: a warp is one row
-  int cur = lab(z0 * nxy + y * nx + x, in);
+  int kc = lab.id(z0 * nxy + y * nx + x, in);
+  int cur = lab.labels_warp(kc, in);
   for (int z = z0; z < z1; ++z) {
     const int row = z * nxy + y * nx;
-    const int s0 = cur;
+    const int s0 = cur, k0 = kc;
     if (seg && in) seg[row + x] = s0;
     const int zn = z + 1 >= nz ? 0 : z + 1;
-    int sz = 0;
-    if (want_pairs || z + 1 < z1) sz = lab(zn * nxy + y * nx + x, in);
+    int kz = 0;
+    if (want_pairs || z + 1 < z1) kz = lab.id(zn * nxy + y * nx + x, in);
     if (want_pairs) {
-      int sx = __shfl_down_sync(0xffffffffu, s0, 1);
-      const int sy = lab(z * nxy + yp * nx + x, in);
-      if (in && (lane == 31 || x + 1 >= nx)) sx = lab_one(lab, row + xp);
+      int kx = __shfl_down_sync(0xffffffffu, k0, 1);
+      const int ky = lab.id(z * nxy + yp * nx + x, in);
+      if (in && (lane == 31 || x + 1 >= nx)) kx = lab.id(row + xp, true);
 #pragma unroll
       for (int dd = 0; dd < 3; ++dd) {
-        const int s1 = dd == 0 ? sx : (dd == 1 ? sy : sz);
+        const int k1 = dd == 0 ? kx : (dd == 1 ? ky : kz);
         uint64_t pk = kEmpty;
-        if (in && s1 != s0) {
-          const int g0 = gb + s0, g1 = gb + s1;
+        if (in && k1 != k0) {
+          const int g0 = gb + s0, g1 = gb + lab.label(k1);
           pk = pair_key(g0, g1);
           lmin = min(lmin, min(g0, g1));
           lmax = max(lmax, max(g0, g1));
@@ -771,7 +783,10 @@ __global__ void __launch_bounds__(STX* STY)
           hash_insert(table, mask, pk, &cnt[CNT_ERR], &cnt[CNT_FLOW_SPARE1]);
       }
     }
-    cur = sz;
+    if (z + 1 < z1) {  // warp-uniform
+      kc = kz;
+      cur = lab.labels_warp(kz, in);
+    }
   }
   if (want_pairs) {
 #pragma unroll
