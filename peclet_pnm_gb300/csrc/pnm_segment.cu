@@ -55,7 +55,7 @@ __device__ __forceinline__ bool key_above(uint32_t o1, uint32_t p1, uint32_t o0,
 }
 
 template <bool ALL_ASCENT, class G, int TZ = 8>
-__global__ void __launch_bounds__(TX* TY, 6)
+__global__ void __launch_bounds__(TX* TY, 8)  // 8 resident tiles per SM (32 registers)
     k_sdf_pass(const float* __restrict__ sdf, G geo, uint8_t* __restrict__ code,
                int* __restrict__ nxt, int* __restrict__ L, uint32_t* __restrict__ peakbits,
                uint32_t* __restrict__ mbits) {
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(RTX* RTY)
       const uint8_t c = cb[tz][ty][lane];
       const int cls = code_cls(c);
       if (cls == CLS_MARKER) {
-        par = ld_relaxed(&L[v]);
+        par = ld_cached(&L[v]);  // the run head, or an ancestor of it
       } else if (cls == CLS_PORE) {
         int li = (tz * RTY + ty) * RTX + lane, moves = 0;
         bool root = false;
