@@ -225,6 +225,7 @@ class Context:
                 rc, f"pnm_ctx_create failed ({rc})"))
         self.h = h
         self.device = int(device) if device >= 0 else None  # None: the device current at creation
+        self.stream_ptr = None  # the caller-owned stream set with set_stream, if any
 
     def check(self, rc: int):
         if rc != PNM_OK:
@@ -232,7 +233,9 @@ class Context:
             raise PnmError(rc, msg or f"pnm error {rc}")
 
     def set_stream(self, stream_ptr: int | None):
+        """Runs this context's work on a caller-owned cudaStream_t (None: its own stream)."""
         self.check(pnm_ctx_set_stream(self.h, stream_ptr or None))
+        self.stream_ptr = stream_ptr or None
 
     def trim(self):
         self.check(pnm_ctx_trim(self.h))

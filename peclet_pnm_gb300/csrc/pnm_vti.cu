@@ -207,6 +207,8 @@ int pnm_read_vti_dev(pnm_ctx* ctx, const char* path, float* d_dst, int64_t n) {
   };
   const int out = body();
   std::fclose(f);
+  // a failed call may leave a staging copy in flight: drain the stream before the buffers go
+  if (out != PNM_OK && (stage[0] || stage[1])) cudaStreamSynchronize(c.stream);
   for (int i = 0; i < 2; ++i) {
     if (done[i]) cudaEventDestroy(done[i]);
     if (stage[i]) cudaFreeHost(stage[i]);

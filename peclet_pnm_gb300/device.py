@@ -66,6 +66,7 @@ class _Stream:
         last = getattr(self.ctx, "_device_last", None)
         if last is not None and last[0] != self.stream.cuda_stream:
             self.stream.wait_event(last[1])
+        self.saved = self.ctx.stream_ptr
         self.ctx.set_stream(self.stream.cuda_stream)
         return self
 
@@ -73,7 +74,7 @@ class _Stream:
         ev = _torch().cuda.Event()
         ev.record(self.stream)
         self.ctx._device_last = (self.stream.cuda_stream, ev)
-        self.ctx.set_stream(None)
+        self.ctx.set_stream(self.saved)  # the stream the caller had set on the context, if any
         self.guard.__exit__(*exc)
 
 

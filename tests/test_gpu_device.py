@@ -237,3 +237,21 @@ def test_network_stats_device_special_values(gpu, torch):
     assert np.array_equal(ds2["coordination"].cpu().numpy(), hs2["coordination"])
     assert ds2["max_abs_flow"] == hs2["max_abs_flow"]
     assert abs(ds2["mean_abs_flow"] - hs2["mean_abs_flow"]) <= 1e-12 * hs2["mean_abs_flow"]
+
+
+def test_device_call_keeps_the_callers_context_stream(gpu, torch):
+    """A device call runs on the current torch stream and then restores the stream the caller had
+    set on the context."""
+    pnm, _ = gpu
+    from peclet_pnm_gb300 import device
+    from peclet_pnm_gb300 import synthetic as syn
+
+    ctx = pnm.Context(0)
+    own = torch.cuda.Stream()
+    ctx.set_stream(own.cuda_stream)
+    sdf = syn.sphere_lattice(36, 30, 24)
+    seg = device.segment_volume_device(torch.from_numpy(sdf).cuda(), [1, 1, 1], ctx=ctx)
+    torch.cuda.synchronize()
+    assert ctx.stream_ptr == own.cuda_stream
+    assert np.array_equal(seg.cpu().numpy().reshape(-1), pnm.segment_volume(sdf, [1, 1, 1], numpy=True))
+    ctx.close()
