@@ -339,7 +339,9 @@ def flow_bench(args, dev):
     modes (|k| <= 8, amplitude 1e-3, seed 4) zeroed in solid, openness clamp(0.5 + face SDF, 0, 1),
     grad_p_zyx = [0, 0, -1e-4]; through the host C ABI (host SDF and fields in, host results out,
     the reference binding's call). Check: the pore residuals of a closed periodic network sum to
-    zero (every throat flux leaves one pore and enters another)."""
+    zero (every throat flux leaves one pore and enters another). `device`: the same call on
+    device-resident inputs (pnm_extract_network_flow_dev, a solver's fields handed over in place),
+    timed with CUDA events on the context's stream."""
     import torch
 
     import peclet_pnm_gb300 as pnm
@@ -349,6 +351,36 @@ def flow_bench(args, dev):
     n = 256
     sdf = syn.packing((n, n, n), 0.4, seed=3, dtype=np.float64, device=dev)
     fields = syn.fourier_fields_device(sdf)
+    o = np.zeros(3, np.float32)
+    s = np.ones(3, np.float32)
+    g = np.array([0.0, 0.0, -1e-4], np.float64)[::-1].copy()  # xyz
+    # device-resident leg
+    d_sdf = sdf.to(torch.float32).contiguous()
+    d_f = [f.contiguous() for f in fields]
+    ctx = pnm.Context(dev.index)
+    stream = torch.cuda.Stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    rd = _capi.PnmFlowResultDev()
+
+    def call_dev():
+        ctx.check(_capi.pnm_extract_network_flow_dev(
+            ctx.h, ctypes.c_void_p(d_sdf.data_ptr()), n, n, n, _capi.as_ptr(o), _capi.as_ptr(s),
+            *[ctypes.c_void_p(f.data_ptr()) for f in d_f], _capi.as_ptr(g), ctypes.byref(rd)))
+
+    for _ in range(3):
+        call_dev()
+    stream.synchronize()
+    reps = 5
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        call_dev()
+    e1.record(stream)
+    e1.synchronize()
+    t_dev = e0.elapsed_time(e1) / 1e3 / reps
+    dev_counts = (int(rd.n_pores), int(rd.n_throats))
+    ctx.set_stream(None)
+    del d_sdf, d_f
     h_sdf = torch.empty((n, n, n), dtype=torch.float32, pin_memory=True)
     h_sdf.copy_(sdf.to(torch.float32))
     hf = []
@@ -358,10 +390,6 @@ def flow_bench(args, dev):
         hf.append(h)
     del sdf, fields
     torch.cuda.empty_cache()
-    ctx = pnm.Context(dev.index)
-    o = np.zeros(3, np.float32)
-    s = np.ones(3, np.float32)
-    g = np.array([0.0, 0.0, -1e-4], np.float64)[::-1].copy()  # xyz
     res = _capi._P(_capi.PnmFlowResult)()
 
     def call():
@@ -389,6 +417,9 @@ def flow_bench(args, dev):
                         "u,v,w,p (seed 4), openness from face SDF, grad_p_zyx [0,0,-1e-4]",
             "e2e": {"value": n ** 3 / t / 1e9, "unit": "Gvoxel/s", "ms_per_step": t * 1e3,
                     "h2d_bytes_per_step": 4 * n ** 3 + 7 * 8 * n ** 3},
+            "device": {"value": n ** 3 / t_dev / 1e9, "unit": "Gvoxel/s",
+                       "ms_per_step": t_dev * 1e3, "h2d_bytes_per_step": 0,
+                       "same_counts": dev_counts == (npo, nth)},
             "pores": npo, "throats": nth,
             "residual_sum_over_flux": float(abs(resid.sum())) / scale}
 
