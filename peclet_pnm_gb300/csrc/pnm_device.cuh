@@ -112,35 +112,6 @@ __device__ __forceinline__ int uf_link(int* L, int a, int b, unsigned* err) {
   return a;
 }
 
-// shared-memory variants (tile-local CCL). Parents strictly decrease along a path, so a find
-// ends within the tile size; the limit only bounds the loop.
-constexpr int kUfLimitShared = 1 << 16;
-__device__ __forceinline__ int uf_find_s(volatile int* L, int x) {
-  for (int it = 0; it < kUfLimitShared; ++it) {
-    const int p = L[x];
-    if (p == x) return x;
-    const int gp = L[p];
-    if (gp != p) L[x] = gp;
-    x = gp;
-  }
-  return x;
-}
-__device__ __forceinline__ void uf_unite_s(int* L, int a, int b) {
-  for (int it = 0; it < kUfLimitShared; ++it) {
-    a = uf_find_s(L, a);
-    b = uf_find_s(L, b);
-    if (a == b) return;
-    if (a < b) {
-      const int t = a;
-      a = b;
-      b = t;
-    }
-    const int old = atomicMin(&L[a], b);
-    if (old == a) return;
-    a = old;
-  }
-}
-
 // Gradient root: follow the ascent pointers (nxt, a voxel id; a local max points at itself) for
 // at most 512 moves (pore_extraction.hpp:277-309 and :626-648; MAX_STEPS = 512).
 __device__ __forceinline__ int chase_root(const int* __restrict__ nxt, int v) {
