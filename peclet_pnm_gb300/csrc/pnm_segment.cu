@@ -400,7 +400,7 @@ __global__ void __launch_bounds__(RTX* RTY)
 // computes its labels into `tmp`, and the next discovery publishes them, so no voxel ever sees a
 // same-sweep label — exactly the double-buffered Jacobi sweep.
 template <class G, int TZ = 8>
-__global__ void __launch_bounds__(TX* TY)
+__global__ void __launch_bounds__(TX* TY, 8)
     k_flood_seed(G geo, const uint8_t* __restrict__ code, int* __restrict__ key, int* L,
                  int* __restrict__ ulist, unsigned* cnt) {
   constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2, NT = TX * TY;
@@ -419,31 +419,45 @@ __global__ void __launch_bounds__(TX* TY)
   if (t < HY) wy[t] = ((Y0 - 1 + t) % ny + ny) % ny;
   if (t < HZ) wz[t] = ((Z0 - 1 + t) % nz + nz) % nz;
   __syncthreads();
-  for (int r = t >> 5; r < HY * HZ; r += NT / 32) {  // one halo row per warp iteration
-    const int hy = r % HY, hz = r / HY;
-    const int rb = wz[hz] * nxy + wy[hy] * nx;
-    const int g0 = rb + wx[lane + 1];
-    const uint8_t c0 = __ldg(&code[g0]);
-    const int k0 = __ldg(&key[g0]);  // independent of the code load
-    mk[hz][hy][lane + 1] = code_cls(c0) == CLS_MARKER ? k0 : INT_MIN;
+  // halo rows, two per warp iteration with all their loads issued before any is used
+  for (int r = t >> 5; r < HY * HZ; r += 2 * (NT / 32)) {
+    const int r2 = r + NT / 32;  // warp-uniform
+    const int rb = wz[r / HY] * nxy + wy[r % HY] * nx;
+    const int rb2 = r2 < HY * HZ ? wz[r2 / HY] * nxy + wy[r2 % HY] * nx : rb;
+    const int hx = lane == 0 ? 0 : HX - 1;
+    const uint8_t c0 = __ldg(&code[rb + wx[lane + 1]]);
+    const int k0 = __ldg(&key[rb + wx[lane + 1]]);
+    const uint8_t c2 = __ldg(&code[rb2 + wx[lane + 1]]);
+    const int k2 = __ldg(&key[rb2 + wx[lane + 1]]);
+    uint8_t c1 = 0, c3 = 0;
+    int k1 = 0, k3 = 0;
     if (lane < 2) {
-      const int hx = lane == 0 ? 0 : HX - 1;
-      const int g1 = rb + wx[hx];
-      const uint8_t c1 = __ldg(&code[g1]);
-      const int k1 = __ldg(&key[g1]);
-      mk[hz][hy][hx] = code_cls(c1) == CLS_MARKER ? k1 : INT_MIN;
+      c1 = __ldg(&code[rb + wx[hx]]);
+      k1 = __ldg(&key[rb + wx[hx]]);
+      c3 = __ldg(&code[rb2 + wx[hx]]);
+      k3 = __ldg(&key[rb2 + wx[hx]]);
+    }
+    mk[r / HY][r % HY][lane + 1] = code_cls(c0) == CLS_MARKER ? k0 : INT_MIN;
+    if (lane < 2) mk[r / HY][r % HY][hx] = code_cls(c1) == CLS_MARKER ? k1 : INT_MIN;
+    if (r2 < HY * HZ) {
+      mk[r2 / HY][r2 % HY][lane + 1] = code_cls(c2) == CLS_MARKER ? k2 : INT_MIN;
+      if (lane < 2) mk[r2 / HY][r2 % HY][hx] = code_cls(c3) == CLS_MARKER ? k3 : INT_MIN;
     }
   }
   __syncthreads();
   const int tx = lane, ty = t >> 5;
   const int gx = X0 + tx, gy = Y0 + ty;
+  const bool inxy = gx < nx && gy < ny;
+  // the next plane's code byte is loaded while this plane's is used
+  uint8_t cnext = (inxy && Z0 < nz) ? __ldg(&code[Z0 * nxy + gy * nx + gx]) : 0;
   for (int tz = 0; tz < TZ; ++tz) {
     const int gz = Z0 + tz;
-    const bool valid = gx < nx && gy < ny && gz < nz;
+    const bool valid = inxy && gz < nz;
     const int ci = gz * nxy + gy * nx + gx;
+    const uint8_t c = cnext;
+    if (tz + 1 < TZ) cnext = (inxy && gz + 1 < nz) ? __ldg(&code[ci + nxy]) : 0;
     bool rest = false;
     if (valid) {
-      const uint8_t c = code[ci];
       if (code_cls(c) == CLS_FLOOD) {
         if (code_seed(c)) {
           int bestk = INT_MIN;  // largest marker key == smallest label
