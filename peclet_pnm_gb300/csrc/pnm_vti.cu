@@ -177,6 +177,14 @@ int pnm_read_vti_dev(pnm_ctx* ctx, const char* path, float* d_dst, int64_t n) {
   auto body = [&]() -> int {
     if (rc != PNM_OK) return fail(rc, why);
     if (cudaSetDevice(c.device) != cudaSuccess) return fail(PNM_ERR_CUDA, "cudaSetDevice");
+    if (n > 0) {  // the destination must be device (or managed) memory
+      cudaPointerAttributes pa{};
+      if (cudaPointerGetAttributes(&pa, d_dst) != cudaSuccess ||
+          (pa.type != cudaMemoryTypeDevice && pa.type != cudaMemoryTypeManaged)) {
+        cudaGetLastError();
+        return fail(PNM_ERR_ARG, "destination is not device memory");
+      }
+    }
     const int64_t avail = std::min<int64_t>(h.bytes, n * 4);  // bytes
     if (std::fseek(f, (long)h.offset, SEEK_SET) != 0) return fail(PNM_ERR_ARG, "seek failed");
     for (int i = 0; i < 2; ++i)

@@ -72,9 +72,9 @@ class SDFReader:
 def read_vti_device(filename, out=None, *, ctx: Context | None = None):
     """Reads the values into device memory without a host-side copy of the volume.
 
-    `out` is a contiguous float32 device buffer exposing ``data_ptr()`` and ``numel()`` (a CUDA
-    tensor) with at least Nz*Ny*Nx elements; when omitted a ``torch`` tensor of shape
-    (Nz,Ny,Nx) is allocated on the context's device. Returns ``(out, origin_zyx, spacing_zyx)``.
+    `out` is a contiguous float32 CUDA tensor with at least Nz*Ny*Nx elements; when omitted a
+    ``torch`` tensor of shape (Nz,Ny,Nx) is allocated on the context's device. Returns
+    ``(out, origin_zyx, spacing_zyx)``.
     The copy runs on the context's stream and is complete when this returns."""
     ctx = ctx or default_context()
     h = read_vti_header(filename)
@@ -86,8 +86,13 @@ def read_vti_device(filename, out=None, *, ctx: Context | None = None):
         import torch
         dev = ctx.device if ctx.device is not None else torch.cuda.current_device()
         out = torch.empty((nz, ny, nx), dtype=torch.float32, device=f"cuda:{dev}")
-    elif int(out.numel()) < n:
-        raise RuntimeError(f"device buffer holds {int(out.numel())} values, the file {n}")
+    else:
+        import torch
+        if not (isinstance(out, torch.Tensor) and out.is_cuda and out.dtype == torch.float32
+                and out.is_contiguous()):
+            raise RuntimeError("out must be a contiguous float32 CUDA tensor")
+        if int(out.numel()) < n:
+            raise RuntimeError(f"device buffer holds {int(out.numel())} values, the file {n}")
     rc = _capi.pnm_read_vti_dev(ctx.h, _path(filename), ctypes.c_void_p(out.data_ptr()), n)
     if rc != _capi.PNM_OK:
         raise PnmError(rc, _capi.pnm_last_error(ctx.h).decode(errors="replace"))

@@ -255,3 +255,17 @@ def test_device_call_keeps_the_callers_context_stream(gpu, torch):
     assert ctx.stream_ptr == own.cuda_stream
     assert np.array_equal(seg.cpu().numpy().reshape(-1), pnm.segment_volume(sdf, [1, 1, 1], numpy=True))
     ctx.close()
+
+
+def test_read_vti_device_rejects_host_destinations(gpu, torch, tmp_path):
+    pnm, ctx = gpu
+    from peclet_pnm_gb300 import _capi
+
+    p = tmp_path / "h.vti"
+    pnm.write_sdf_vti(str(p), np.ones((2, 3, 4), np.float32))
+    with pytest.raises(RuntimeError, match="CUDA tensor"):
+        pnm.read_vti_device(str(p), torch.zeros(24))
+    host = torch.zeros(24, pin_memory=True)
+    rc = _capi.pnm_read_vti_dev(ctx.h, str(p).encode(), host.data_ptr(), 24)
+    assert rc == _capi.PNM_ERR_ARG
+    assert host.sum().item() == 0.0
