@@ -76,23 +76,23 @@ def read_vti_device(filename, out=None, *, ctx: Context | None = None):
     ``torch`` tensor of shape (Nz,Ny,Nx) is allocated on the context's device. Returns
     ``(out, origin_zyx, spacing_zyx)``.
     The copy runs on the context's stream and is complete when this returns."""
-    ctx = ctx or default_context()
+    import torch
+
     h = read_vti_header(filename)
     nx, ny, nz = h["dims_xyz"]
     if nx < 0 or ny < 0 or nz < 0:
         raise RuntimeError("negative extent in VTI header")
     n = nx * ny * nz
-    if out is None:
-        import torch
-        dev = ctx.device if ctx.device is not None else torch.cuda.current_device()
-        out = torch.empty((nz, ny, nx), dtype=torch.float32, device=f"cuda:{dev}")
-    else:
-        import torch
+    if out is not None:
         if not (isinstance(out, torch.Tensor) and out.is_cuda and out.dtype == torch.float32
                 and out.is_contiguous()):
             raise RuntimeError("out must be a contiguous float32 CUDA tensor")
         if int(out.numel()) < n:
             raise RuntimeError(f"device buffer holds {int(out.numel())} values, the file {n}")
+    ctx = ctx or default_context()
+    if out is None:
+        dev = ctx.device if ctx.device is not None else torch.cuda.current_device()
+        out = torch.empty((nz, ny, nx), dtype=torch.float32, device=f"cuda:{dev}")
     rc = _capi.pnm_read_vti_dev(ctx.h, _path(filename), ctypes.c_void_p(out.data_ptr()), n)
     if rc != _capi.PNM_OK:
         raise PnmError(rc, _capi.pnm_last_error(ctx.h).decode(errors="replace"))
