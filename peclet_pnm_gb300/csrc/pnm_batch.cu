@@ -345,7 +345,7 @@ Status wait_checked(pnm_batch& b) {
       hc *= 4;
       grow = true;
     }
-    const long long peaks = b.plan.h_cnt[pnm::CNT_FLOW_SPARE0];
+    const long long peaks = b.plan.h_cnt[pnm::CNT_PEAKS];
     if (peaks > pc) {
       pc = peaks + peaks / 8 + 1024;
       grow = true;
@@ -782,8 +782,8 @@ int pnm_batch_get_stats(const pnm_batch* b, pnm_stats* out) {
     const unsigned* h = b->plan.h_cnt;
     out->ccl_edges = h[pnm::CNT_EDGES];
     out->flood_sweeps = (int32_t)h[pnm::CNT_SWEEPS];
-    out->n_pores = h[pnm::CNT_FLOW_SPARE0];
-    out->n_pairs = h[pnm::CNT_FLOW_SPARE1];
+    out->n_pores = h[pnm::CNT_PEAKS];
+    out->n_pairs = h[pnm::CNT_PAIRS];
     int64_t np = 0, ns = 0;
     for (size_t i = 0; i < b->lay.vols.size(); ++i) {
       np += b->plan.h_res[i].n_pore_labels;

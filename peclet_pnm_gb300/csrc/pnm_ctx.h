@@ -48,10 +48,10 @@ enum Counter : int {
   CNT_KEYS,          // distinct basin / solid keys seen (keylist length)
   CNT_FRONT0,        // flood frontier length, ping
   CNT_FRONT1,        // flood frontier length, pong
-  CNT_FRONT_SPARE,   // flood voxels without a marker neighbour (list U)
+  CNT_ULIST,         // flood voxels without a marker neighbour (list U)
   CNT_EDGES,         // marker-CCL links united (run pairs that touch)
-  CNT_FLOW_SPARE0,
-  CNT_FLOW_SPARE1,
+  CNT_PEAKS,         // batch: extract_pores peaks over all volumes
+  CNT_PAIRS,         // distinct label pairs in the hash set
   CNT_SWEEPS,        // flood sweeps run by the persistent flood loop
   CNT_BAR0,          // grid barrier of the persistent flood loop: arrivals
   CNT_BAR1,          //   and generation

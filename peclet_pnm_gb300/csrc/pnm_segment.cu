@@ -475,7 +475,7 @@ __global__ void __launch_bounds__(TX* TY, 8)
         }
       }
     }
-    const int pos = warp_append(&cnt[CNT_FRONT_SPARE], rest);
+    const int pos = warp_append(&cnt[CNT_ULIST], rest);
     if (rest) ulist[pos] = off + ci;
   }
 }
@@ -794,7 +794,7 @@ __global__ void __launch_bounds__(STX* STY)
         }
         const uint64_t pp = __shfl_up_sync(0xffffffffu, pk, 1);
         if (pk != kEmpty && (lane == 0 || pp != pk))
-          hash_insert(table, mask, pk, &cnt[CNT_ERR], &cnt[CNT_FLOW_SPARE1]);
+          hash_insert(table, mask, pk, &cnt[CNT_ERR], &cnt[CNT_PAIRS]);
       }
     }
     if (z + 1 < z1) {  // warp-uniform
@@ -1003,7 +1003,7 @@ __global__ void k_batch_tail(const VolDesc* __restrict__ v, VolResult* r, int nv
                              const uint64_t* __restrict__ keys, const unsigned* m_p,
                              const int* range, int b, unsigned* cnt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) cnt[CNT_FLOW_SPARE0] = peakpref[words];
+  if (i == 0) cnt[CNT_PEAKS] = peakpref[words];
   if (i >= nvol) return;
   const long long off = v[i].off, n = (long long)v[i].nx * v[i].ny * v[i].nz;
   const long long w0 = off >> 5, w1 = (off + n + 31) >> 5;
@@ -1159,7 +1159,7 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
                                                                       key, keylist, c.d_cnt);
   k_flood_seed<OneVol, TZ_PLAIN><<<tiles, TX * TY, 0, s>>>(geo, st->code, key, L, ulist, c.d_cnt);
   const unsigned fgrid = grid_for(n, 256, c.sm_count, 4);
-  k_flood_layer2<<<fgrid, 256, 0, s>>>(geo, st->code, key, ulist, &c.d_cnt[CNT_FRONT_SPARE], f0,
+  k_flood_layer2<<<fgrid, 256, 0, s>>>(geo, st->code, key, ulist, &c.d_cnt[CNT_ULIST], f0,
                                        &c.d_cnt[CNT_FRONT0]);
   c.launches += 4;
   PNM_CUDA(cudaGetLastError());
@@ -1248,7 +1248,7 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
     const int init[2] = {INT_MAX, INT_MIN};
     PNM_CUDA(cudaMemcpyAsync(range, init, sizeof(init), cudaMemcpyHostToDevice, s));
     PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_ERR], 0, sizeof(unsigned), s));
-    PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_FLOW_SPARE1], 0, sizeof(unsigned), s));
+    PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_PAIRS], 0, sizeof(unsigned), s));
     const unsigned g = (unsigned)boxes_of(d, STX, STY, STZ);
     OneVol geo{d, 0.0f};
     // labels already on their way to the host (an earlier attempt) are not written again
@@ -1291,7 +1291,7 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
       cap <<= 2;
       continue;
     }
-    const long long m = c.h_cnt[CNT_FLOW_SPARE1];
+    const long long m = c.h_cnt[CNT_PAIRS];
     *n_pairs = m;
     int32_t* out = nullptr;
     PNM_TRY(c.buf(S_PAIRS, 2 * m + 2, &out));
@@ -1393,7 +1393,7 @@ Status enqueue_batch(BatchPlan& p, cudaStream_t s, long long* launches) {
       k_flood_seed<VolTab, 8><<<tiles, TX * TY, 0, s>>>(geo, p.code, p.key, p.L, p.ulist, p.cnt);
   }
   k_flood_layer2<<<grid_for(n, 256, sm, 4), 256, 0, s>>>(
-      geo, p.code, p.key, p.ulist, &p.cnt[CNT_FRONT_SPARE], p.f0, &p.cnt[CNT_FRONT0]);
+      geo, p.code, p.key, p.ulist, &p.cnt[CNT_ULIST], p.f0, &p.cnt[CNT_FRONT0]);
   *launches += 6;
   PNM_CUDA(cudaGetLastError());
   PNM_CUDA(launch_flood_loop(geo, p.code, p.key, p.L, p.f0, p.f1, p.tmp, p.cnt, p.max_sweeps, sm,
