@@ -16,8 +16,10 @@ roofline: the whole pipeline against the 64 B/voxel algorithmic model of the ext
          measured HBM copy bandwidth.
 N > 1  : independent replicas, one volume per rank (the path does not shard): scaling "weak".
 --impl reference: the reference's CPU implementation on this host's cores (the reference header
-         built against the Kokkos shim when present here, otherwise the project's CPU restatement),
-         each step a bounded sub-volume of the same workload.
+         built against the Kokkos shim where its checkout exists, otherwise the project's C++
+         restatement of it), each step one extract_pore_network of the same 512^3 volume. This
+         arm never loads the product library: the volume comes from the generator module loaded
+         by path (torch on the GPU when present, numpy otherwise).
 """
 from __future__ import annotations
 
@@ -48,10 +50,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=512, help="cube edge of the benchmark volume")
-    ap.add_argument("--cpu-sample", type=int, default=384,
-                    help="cube edge of the bounded CPU baseline sample")
-    ap.add_argument("--ref-sample", type=int, default=256,
-                    help="cube edge of one reference-arm step")
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="cube edge of the CPU baseline sample (0: the whole benchmark volume)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the ragged 96-volume batched-vs-plain measurement")
@@ -157,10 +157,20 @@ def whole_job_rate(local_value: float, voxels_per_rank: int, world: int, device)
     return worst, voxels_per_rank * world / worst / 1e9
 
 
-def gen_volume(n_edge, seed, device):
-    from peclet_pnm_gb300 import synthetic as syn
+def load_synthetic():
+    """peclet_pnm_gb300/synthetic.py loaded by path: numpy / torch only, so the reference arm
+    gets the benchmark volume without importing the package (which loads the CUDA library)."""
+    import importlib.util
 
-    return syn.packing((n_edge, n_edge, n_edge), 0.4, seed=seed, device=device)
+    spec = importlib.util.spec_from_file_location(
+        "pnm_synthetic", os.path.join(ROOT, "peclet_pnm_gb300", "synthetic.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def gen_volume(n_edge, seed, device):
+    return load_synthetic().packing((n_edge, n_edge, n_edge), 0.4, seed=seed, device=device)
 
 
 def cpu_sample_run(n_edge, threads, kind, sdf_np):
@@ -191,15 +201,20 @@ def reference_arm(args, rank):
 
     kind = "reference" if reference_available() else "port"
     threads = os.cpu_count() or 1
-    sdf = sample_volume(args.ref_sample, 2)
+    # the volume `ours` times at N=1 (rank 0's replica seed), whole, every step
+    sdf = sample_volume(args.size, replica_seed(0))
     vox = sdf.size
     for _ in range(args.warmup):
-        cpu_sample_run(args.ref_sample, threads, kind, sdf)
-    ts = [cpu_sample_run(args.ref_sample, threads, kind, sdf) for _ in range(args.steps)]
+        cpu_sample_run(args.size, threads, kind, sdf)
+    ts = [cpu_sample_run(args.size, threads, kind, sdf) for _ in range(args.steps)]
     t = sum(ts) / len(ts)
     value = vox / t / 1e9
-    sample = (f"{args.ref_sample}^3 sub-volume of the same packing generator per step "
-              f"({'reference header + Kokkos-compat OpenMP shim' if kind == 'reference' else 'C++ restatement of the reference algorithm, OpenMP'})")
+    impl = ("the reference's src/pore_extraction.hpp built against the project's Kokkos-compat "
+            "OpenMP shim" if kind == "reference" else
+            "the project's C++ restatement of the reference algorithm (OpenMP); the reference "
+            "checkout is absent on this host")
+    sample = (f"the whole {args.size}^3 benchmark volume (seed {replica_seed(0)}) per step, "
+              f"one extract_pore_network on {threads} host threads: {impl}")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Gvoxel/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
@@ -671,13 +686,16 @@ def ours(args, rank, world, local_rank):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        samp = sdf.cpu().numpy()[:args.cpu_sample, :args.cpu_sample, :args.cpu_sample].copy()
-        t_cpu = cpu_sample_run(args.cpu_sample, threads, "port", samp)
+        e = args.cpu_sample or n_edge
+        samp = sdf.cpu().numpy()[:e, :e, :e].copy()
+        t_cpu = cpu_sample_run(e, threads, "port", samp)
+        what = (f"the whole {e}^3 benchmark volume" if e == n_edge else
+                f"{e}^3 corner of the benchmark volume")
         result["cpu_baseline"] = {
             "value": samp.size / t_cpu / 1e9, "unit": "Gvoxel/s", "cores": threads,
             "kind": "port",
-            "sample": f"{args.cpu_sample}^3 corner of the benchmark volume, one "
-                      f"extract_pore_network ({t_cpu:.1f} s, C++ restatement with OpenMP)"}
+            "sample": f"{what}, one extract_pore_network ({t_cpu:.1f} s, the project's C++ "
+                      f"restatement of the reference algorithm, OpenMP on {threads} threads)"}
     ctx.close()
     del sdf
     torch.cuda.empty_cache()

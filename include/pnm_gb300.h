@@ -58,12 +58,27 @@ const char* pnm_execution_space(void);
 /* Frees buffers returned by the host entry points. */
 void pnm_free(void* p);
 
+/* Stages of a call, named after the reference's kernel labels (src/pore_extraction.hpp:86-884).
+ * Every stage is enclosed in an NVTX range of that name (visible to Nsight tools; a no-op
+ * otherwise); with timing on, pnm_stats.stage_ms holds each stage's device time in the last call. */
+#define PNM_STAGE_SDF_PASS 0      /* "pnm::extract_pores" + "pnm::init_markers": one pass over the
+                                     SDF (peaks, classes, ascent directions, marker runs) */
+#define PNM_STAGE_MERGE_MARKERS 1 /* "pnm::merge_markers": marker CCL */
+#define PNM_STAGE_GRADIENT_PATH 2 /* "pnm::gradient_path": basin roots (and marker roots) */
+#define PNM_STAGE_FLOOD 3         /* "pnm::flood": Jacobi sweeps over the shallow solid */
+#define PNM_STAGE_RELABEL 4       /* "pnm::relabel_min" .. "pnm::relabel_assign": label ids */
+#define PNM_STAGE_SEG_PAIRS 5     /* "pnm::relabel_seg" + "pnm::boundary_pairs" */
+#define PNM_STAGE_PAIR_SORT 6     /* unique sorted pairs (the reference sorts on the host) */
+#define PNM_STAGE_PORES 7         /* pore records with their centroids */
+#define PNM_STAGE_NETWORK_FLOW 8  /* "nf::*": network flow after the segmentation */
+#define PNM_STAGE_COUNT 9
+
 /* Per-context statistics: cumulative counters and figures of the last call. */
 typedef struct {
   int64_t launches;        /* CUDA kernels launched by this context since creation */
   int64_t calls;           /* entry-point calls since creation */
   int64_t voxels;          /* last call: nx*ny*nz */
-  int64_t ccl_edges;       /* last call: marker-CCL edges emitted by the SDF pass */
+  int64_t ccl_edges;       /* last call: marker-CCL links united (run pairs that touch) */
   int32_t flood_sweeps;    /* last call: Jacobi flood sweeps run (incl. the empty final one) */
   int32_t n_pore_labels;   /* last call: pore labels (np) */
   int32_t n_solid_labels;  /* last call: solid labels */
@@ -71,8 +86,20 @@ typedef struct {
   int64_t n_pores;         /* last call: extract_pores peaks */
   int64_t n_pairs;         /* last call: unique connections */
   int64_t workspace_bytes; /* device workspace currently held */
+  double stage_ms[PNM_STAGE_COUNT]; /* last call, timing on: device ms per PNM_STAGE_* (0 off) */
 } pnm_stats;
 int pnm_ctx_get_stats(const pnm_ctx* ctx, pnm_stats* out);
+/* Per-stage device timing (CUDA events on the context's stream around each stage), off by
+ * default: on, every call also waits for its last stage before it returns. */
+int pnm_ctx_set_timing(pnm_ctx* ctx, int32_t on);
+
+/* Bounded device waits. The persistent flood loop's grid barrier (the fixpoint of
+ * pore_extraction.hpp:237-269 in one launch) waits at most limit_ns of GPU time per barrier
+ * (default 1e9, 1 s; 1 .. 6e10 accepted); when a wait runs out the kernel returns and the call
+ * fails with PNM_ERR_NOT_CONVERGED, and the context stays usable. extra_arrivals > 0 makes every
+ * barrier wait for that many arrivals that never come, so its wait runs out: a test of that error
+ * path without a device fault. 0 in normal use. */
+int pnm_ctx_set_wait_limit(pnm_ctx* ctx, int64_t limit_ns, int32_t extra_arrivals);
 
 /* ---- host-pointer entry points ------------------------------------------------------------ */
 
@@ -203,8 +230,12 @@ int pnm_flow_stats_dev(pnm_ctx* ctx, const pnm_flow_result_dev* r, double* d_con
  * loads the library until the process exits), so volumes above 2^26 voxels (67,108,864, e.g.
  * 406^3) are rejected with PNM_ERR_SHAPE. All calls on a device share that array: calls whose
  * work overlaps on the GPU race and must be serialised. The first call on each device looks up
- * the array's address; make it before any stream capture. Returns PNM_ERR_CAPACITY (with
- * *n_pores = the count found) when pore_cap is too small. No context is used or needed. */
+ * the array's address; under CUDA's lazy module loading (the default since CUDA 12.2) that first
+ * call is also when the driver loads the library's kernels on the device and reserves the array,
+ * which allocates and may synchronise. So make the first call at start-up, before the caller's
+ * pool claims the device's memory and before any stream capture (or run with
+ * CUDA_MODULE_LOADING=EAGER). Returns PNM_ERR_CAPACITY (with *n_pores = the count found, and
+ * only the first pore_cap records written) when pore_cap is too small. No context is used. */
 int pnm_extract_pores_noalloc(const float* d_sdf, int32_t nx, int32_t ny, int32_t nz,
                               const float origin_xyz[3], const float spacing_xyz[3],
                               pnm_pore* d_pores, int64_t pore_cap, int64_t* n_pores,

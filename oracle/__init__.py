@@ -42,7 +42,9 @@ class _FlowResult(ctypes.Structure):
 
 class _PortFlowResult(ctypes.Structure):
     _fields_ = _FlowResult._fields_ + [("throat_root", _P(ctypes.c_longlong)),
-                                       ("pore_peak", _P(ctypes.c_int32))]
+                                       ("pore_peak", _P(ctypes.c_int32)),
+                                       ("throat_absflow", _P(ctypes.c_double)),
+                                       ("pore_absflux", _P(ctypes.c_double))]
 
 
 def _arr(ptr, count, dtype):
@@ -200,6 +202,10 @@ class Oracle:
         if self.kind == "port":
             out["throat_root"] = _arr(c.throat_root, nt, np.int64)
             out["pore_peak"] = _arr(c.pore_peak, npo, np.int32)
+            # sums of |q| over each throat's and each pore's terms: the per-element scale of the
+            # rounding error of those cancelling sums
+            out["throat_absflow"] = _arr(c.throat_absflow, nt, np.float64)
+            out["pore_absflux"] = _arr(c.pore_absflux, npo, np.float64)
         self._f_flowfree(r)
         return out
 

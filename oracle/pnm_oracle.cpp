@@ -639,6 +639,8 @@ pnmo_flow_result* network_flow(const float* sdf, Dims r, const float* org, const
 
   // throat fluxes, areas, centroid moments; per-pore residual (:866-944)
   std::vector<double> Q(nt, 0.0), A(nt, 0.0), Cx(nt, 0.0), Cy(nt, 0.0), Cz(nt, 0.0), resid(np, 0.0);
+  // sums of |q| over the same terms: the per-element scale of a cancelling sum's rounding error
+  std::vector<double> absQ(nt, 0.0), absR(np, 0.0);
   {
     const double Ax = double(spc[1]) * spc[2], Ay = double(spc[0]) * spc[2],
                  Az = double(spc[0]) * spc[1];
@@ -662,6 +664,8 @@ pnmo_flow_result* network_flow(const float* sdf, Dims r, const float* org, const
             const double q = opn * vel * area;
             if (a > 0) aadd(&resid[a - 1], q);
             if (b > 0) aadd(&resid[b - 1], -q);
+            if (a > 0) aadd(&absR[a - 1], std::fabs(q));
+            if (b > 0) aadd(&absR[b - 1], std::fabs(q));
             const long long rt = fpar[3 * (long long)c + d];
             if (rt >= 0) {
               long long l = 0, hgh = ntl - 1, slot = -1;
@@ -680,6 +684,7 @@ pnmo_flow_result* network_flow(const float* sdf, Dims r, const float* org, const
               if (slot >= 0) {
                 const double w0 = opn * area;
                 aadd(&Q[slot], a < b ? q : -q);
+                aadd(&absQ[slot], std::fabs(q));
                 aadd(&A[slot], w0);
                 const int pk = peak[lo - 1];
                 const int pkx = pk % r.x, pky = (pk / r.x) % r.y, pkz = pk / (r.x * r.y);
@@ -752,6 +757,8 @@ pnmo_flow_result* network_flow(const float* sdf, Dims r, const float* org, const
   // per-throat patch root fid and peak voxels, exposed for stage-level parity checks
   res->throat_root = dup(rootF);
   res->pore_peak = dup(peak);
+  res->throat_absflow = dup(absQ);
+  res->pore_absflux = dup(absR);
   return res;
 }
 
@@ -779,6 +786,8 @@ void pnmo_flow_result_free(pnmo_flow_result* r) {
   std::free(r->throat_dp);
   std::free(r->throat_root);
   std::free(r->pore_peak);
+  std::free(r->throat_absflow);
+  std::free(r->pore_absflux);
   std::free(r);
 }
 

@@ -23,6 +23,8 @@ typedef struct {
   double* throat_dp;
   long long* throat_root; /* patch root face id per throat */
   int32_t* pore_peak;     /* basin peak voxel per pore label (0 when none) */
+  double* throat_absflow; /* sum of |q| over the faces of each throat (tolerance scale) */
+  double* pore_absflux;   /* sum of |q| over the faces each pore residual sums */
 } pnmo_flow_result;
 
 void pnmo_free(void* p);

@@ -61,11 +61,16 @@ class PnmFlowResult(ctypes.Structure):
                 ("throat_area", _P(ctypes.c_double)), ("throat_dp", _P(ctypes.c_double))]
 
 
+#: PNM_STAGE_* in order: the reference kernel labels each stage covers
+STAGES = ["sdf_pass", "merge_markers", "gradient_path", "flood", "relabel", "seg_pairs",
+          "pair_sort", "pores", "network_flow"]
+
+
 class PnmStats(ctypes.Structure):
     _fields_ = [("launches", _i64), ("calls", _i64), ("voxels", _i64), ("ccl_edges", _i64),
                 ("flood_sweeps", _i32), ("n_pore_labels", _i32), ("n_solid_labels", _i32),
                 ("reserved", _i32), ("n_pores", _i64), ("n_pairs", _i64),
-                ("workspace_bytes", _i64)]
+                ("workspace_bytes", _i64), ("stage_ms", ctypes.c_double * len(STAGES))]
 
 
 def _sig(name, res, *args):
@@ -82,6 +87,8 @@ pnm_ctx_set_stream = _sig("pnm_ctx_set_stream", ctypes.c_int, _vp, _vp)
 pnm_ctx_trim = _sig("pnm_ctx_trim", ctypes.c_int, _vp)
 pnm_execution_space = _sig("pnm_execution_space", ctypes.c_char_p)
 pnm_ctx_get_stats = _sig("pnm_ctx_get_stats", ctypes.c_int, _vp, _P(PnmStats))
+pnm_ctx_set_timing = _sig("pnm_ctx_set_timing", ctypes.c_int, _vp, _i32)
+pnm_ctx_set_wait_limit = _sig("pnm_ctx_set_wait_limit", ctypes.c_int, _vp, _i64, _i32)
 pnm_free = _sig("pnm_free", None, _vp)
 pnm_extract_pores = _sig("pnm_extract_pores", ctypes.c_int, _vp, _vp, _i32, _i32, _i32, _vp, _vp,
                          _P(_P(PnmPore)), _P(_i64))
@@ -193,7 +200,8 @@ EXPORTED = ["pnm_ctx_create", "pnm_ctx_destroy", "pnm_last_error", "pnm_ctx_set_
             "pnm_ctx_trim", "pnm_execution_space", "pnm_free", "pnm_extract_pores",
             "pnm_segment_volume", "pnm_extract_topology", "pnm_extract_pore_network",
             "pnm_extract_network_flow", "pnm_flow_result_free", "pnm_extract_pore_network_dev",
-            "pnm_segment_volume_dev", "pnm_ctx_get_stats", "pnm_extract_pores_noalloc",
+            "pnm_segment_volume_dev", "pnm_ctx_get_stats", "pnm_ctx_set_timing",
+            "pnm_ctx_set_wait_limit", "pnm_extract_pores_noalloc",
             "pnm_batch_plan_bytes", "pnm_batch_create", "pnm_batch_destroy",
             "pnm_batch_last_error", "pnm_batch_stream", "pnm_batch_set_sdf", "pnm_batch_sdf_dev",
             "pnm_batch_launch", "pnm_batch_wait", "pnm_batch_run", "pnm_batch_volume_info",
@@ -241,9 +249,23 @@ class Context:
         self.check(pnm_ctx_trim(self.h))
 
     def stats(self) -> dict:
+        """Cumulative counters and the last call's figures; ``stage_ms`` maps each stage to its
+        device time in the last call (zeros unless timing is on)."""
         st = PnmStats()
         self.check(pnm_ctx_get_stats(self.h, ctypes.byref(st)))
-        return {k: getattr(st, k) for k, _ in PnmStats._fields_ if k != "reserved"}
+        out = {k: getattr(st, k) for k, _ in PnmStats._fields_
+               if k not in ("reserved", "stage_ms")}
+        out["stage_ms"] = {name: float(st.stage_ms[i]) for i, name in enumerate(STAGES)}
+        return out
+
+    def set_timing(self, on: bool = True):
+        """Per-stage device timing (CUDA events) of every following call."""
+        self.check(pnm_ctx_set_timing(self.h, 1 if on else 0))
+
+    def set_wait_limit(self, limit_ns: int = 1_000_000_000, extra_arrivals: int = 0):
+        """Limit of each bounded device wait (the flood loop's grid barrier). extra_arrivals > 0
+        makes those waits run out on purpose (tests of the error path); 0 in normal use."""
+        self.check(pnm_ctx_set_wait_limit(self.h, int(limit_ns), int(extra_arrivals)))
 
     def close(self):
         if getattr(self, "h", None):

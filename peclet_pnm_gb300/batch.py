@@ -168,7 +168,8 @@ class Batch:
     def stats(self) -> dict:
         st = _capi.PnmStats()
         self.check(_capi.pnm_batch_get_stats(self.h, ctypes.byref(st)))
-        return {k: getattr(st, k) for k, _ in _capi.PnmStats._fields_ if k != "reserved"}
+        return {k: getattr(st, k) for k, _ in _capi.PnmStats._fields_
+                if k not in ("reserved", "stage_ms")}
 
     def close(self):
         if getattr(self, "h", None):

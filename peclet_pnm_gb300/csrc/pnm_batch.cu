@@ -338,7 +338,10 @@ Status wait_checked(pnm_batch& b) {
       return Status{PNM_ERR_NOT_CONVERGED, "union-find exceeded its iteration limit"};
     if (err & pnm::ERRF_FLOOD_LIMIT) return Status{PNM_ERR_NOT_CONVERGED, "flood did not converge"};
     if (err & pnm::ERRF_BARRIER)
-      return Status{PNM_ERR_INTERNAL, "persistent flood loop: grid barrier timed out"};
+      return Status{PNM_ERR_NOT_CONVERGED,
+                    "flood loop: a grid barrier wait ran out (blocks not all resident?)"};
+    if (err & pnm::ERRF_LABEL_RANGE)
+      return Status{PNM_ERR_INTERNAL, "renumbering: a label minimum is outside the volume"};
     long long hc = b.lay.hash_cap, pc = b.lay.pore_cap;
     bool grow = false;
     if (err & pnm::ERRF_HASH_FULL) {

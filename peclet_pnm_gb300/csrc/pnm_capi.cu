@@ -3,6 +3,7 @@
 // sequencing of the device stages. No CPU fallback: without an sm_103 device every entry point
 // returns PNM_ERR_NO_DEVICE.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -79,6 +80,60 @@ Status Ctx::read_counters() {
   return Status::ok();
 }
 
+void Ctx::call_begin() {
+  for (double& t : last.stage_ms) t = 0.0;
+  tstage.clear();
+}
+
+void Ctx::stage_begin(int id, const char* name) {
+  nvtxRangePushA(name);
+  ++nvtx_depth;
+  if (!timing) return;
+  const size_t k = tstage.size();
+  while (tev.size() < 2 * k + 2) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    tev.push_back(e);
+  }
+  if (cudaEventRecord(tev[2 * k], stream) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  tstage.push_back(id);
+}
+
+void Ctx::stage_end() {
+  if (timing && !tstage.empty()) {
+    const size_t k = tstage.size() - 1;
+    if (cudaEventRecord(tev[2 * k + 1], stream) != cudaSuccess) cudaGetLastError();
+  }
+  if (nvtx_depth > 0) {
+    nvtxRangePop();
+    --nvtx_depth;
+  }
+}
+
+void Ctx::stage_collect() {
+  if (!timing || tstage.empty()) return;
+  if (cudaEventSynchronize(tev[2 * tstage.size() - 1]) != cudaSuccess) {
+    cudaGetLastError();
+    tstage.clear();
+    return;
+  }
+  for (size_t k = 0; k < tstage.size(); ++k) {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, tev[2 * k], tev[2 * k + 1]) == cudaSuccess &&
+        tstage[k] >= 0 && tstage[k] < PNM_STAGE_COUNT)
+      last.stage_ms[tstage[k]] += ms;
+    else
+      cudaGetLastError();
+  }
+  tstage.clear();
+}
+
 Status check_dims(Dims d, const float* spacing, bool need_spacing) {
   if (d.nx < 0 || d.ny < 0 || d.nz < 0) return Status{PNM_ERR_ARG, "dims must be non-negative"};
   // voxel ids, labels and the first-appearance sentinel are int32 (get_idx returns int,
@@ -104,6 +159,7 @@ namespace {
 
 int finish(pnm_ctx* ctx, Status s) {
   ++ctx->c.calls;
+  ctx->c.stage_collect();
   if (!s.good()) ctx->c.last_error = s.msg;
   return s.code;
 }
@@ -111,6 +167,7 @@ int finish(pnm_ctx* ctx, Status s) {
 Status enter(Ctx& c) {
   const cudaError_t e = cudaSetDevice(c.device);
   if (e != cudaSuccess) return pnm::cuda_status(e, "cudaSetDevice");
+  c.call_begin();
   return Status::ok();
 }
 
@@ -212,6 +269,7 @@ void pnm_ctx_destroy(pnm_ctx* ctx) {
     cudaStreamDestroy(c.copy_stream);
   }
   for (cudaEvent_t e : c.events) cudaEventDestroy(e);
+  for (cudaEvent_t e : c.tev) cudaEventDestroy(e);
   if (c.own_stream) cudaStreamDestroy(c.own_stream);
   delete ctx;
 }
@@ -224,6 +282,19 @@ int pnm_ctx_get_stats(const pnm_ctx* ctx, pnm_stats* out) {
   out->launches = ctx->c.launches;
   out->calls = ctx->c.calls;
   out->workspace_bytes = (int64_t)ctx->c.ws.total_bytes();
+  return PNM_OK;
+}
+
+int pnm_ctx_set_timing(pnm_ctx* ctx, int32_t on) {
+  if (!ctx) return PNM_ERR_ARG;
+  ctx->c.timing = on != 0;
+  return PNM_OK;
+}
+
+int pnm_ctx_set_wait_limit(pnm_ctx* ctx, int64_t limit_ns, int32_t extra_arrivals) {
+  if (!ctx || limit_ns < 1 || limit_ns > 60000000000ll || extra_arrivals < 0) return PNM_ERR_ARG;
+  ctx->c.wait_ns = (unsigned long long)limit_ns;
+  ctx->c.wait_extra = (unsigned)extra_arrivals;
   return PNM_OK;
 }
 

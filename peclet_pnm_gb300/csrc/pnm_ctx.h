@@ -40,6 +40,7 @@ enum ErrFlag : unsigned {
   ERRF_FLOOD_LIMIT = 4u,    // the flood wavefront exceeded its sweep limit
   ERRF_FACE_LIMIT = 8u,     // a face-CCL find/unite exceeded its iteration limit
   ERRF_BARRIER = 16u,       // a grid barrier of a persistent kernel timed out
+  ERRF_LABEL_RANGE = 32u,   // renumbering met a key or label minimum outside the volume
 };
 
 // ---- counter block (device ints; one copy per context) ------------------------------------------
@@ -95,6 +96,20 @@ struct Ctx {
   long long launches = 0;   // kernels launched by this context (cumulative)
   long long calls = 0;      // entry-point calls (cumulative)
   pnm_stats last{};         // per-call statistics of the last call
+  // bounded device waits (pnm_ctx_set_wait_limit): grid-barrier limit in ns of GPU global time,
+  // and arrivals beyond the grid that a barrier waits for (0; > 0 only to test the error path)
+  unsigned long long wait_ns = 1000000000ull;
+  unsigned wait_extra = 0;
+  // stages (PNM_STAGE_*): an NVTX range each, and with timing on a pair of CUDA events on the
+  // stream around each, summed per stage into last.stage_ms when the call ends
+  bool timing = false;
+  std::vector<cudaEvent_t> tev;  // event pool, two per recorded stage interval
+  std::vector<int> tstage;       // stage id of each recorded interval
+  int nvtx_depth = 0;
+  void call_begin();                           // clears the last call's stage times
+  void stage_begin(int id, const char* name);  // NVTX push (+ start event)
+  void stage_end();                            // (end event +) NVTX pop
+  void stage_collect();                        // waits for the events, fills last.stage_ms
   std::string last_error;
   Status fail(Status s) {
     last_error = s.msg;
@@ -109,6 +124,20 @@ struct Ctx {
   }
   Status read_counters();  // synchronises the stream and copies d_cnt -> h_cnt
   Status ensure_copy_events(int n);  // creates the copy stream and at least n events
+};
+
+// One stage of a call for the lifetime of the scope (early returns included); next() ends it
+// and opens the following stage in the same scope.
+struct StageScope {
+  Ctx& c;
+  StageScope(Ctx& ctx, int id, const char* name) : c(ctx) { c.stage_begin(id, name); }
+  void next(int id, const char* name) {
+    c.stage_end();
+    c.stage_begin(id, name);
+  }
+  ~StageScope() { c.stage_end(); }
+  StageScope(const StageScope&) = delete;
+  StageScope& operator=(const StageScope&) = delete;
 };
 
 // Host buffers of a host-pointer call. With them the stages overlap the transfers with the

@@ -125,9 +125,11 @@ __device__ __forceinline__ int chase_root(const int* __restrict__ nxt, int v) {
 }
 
 // ---- grid barrier for persistent (cooperatively launched) kernels ---------------------------------
-// bar[0] counts arrivals, bar[1] is the generation. Every wait is bounded: after kBarrierNs of
-// global time the waiting block sets ERRF_BARRIER and returns false, so a kernel whose blocks were
-// not all resident ends with an error status instead of spinning.
+// bar[0] counts arrivals, bar[1] is the generation. Every wait is bounded: after `limit_ns` of
+// global time (kBarrierNs unless the context sets another limit) the waiting block sets
+// ERRF_BARRIER and returns false, so a kernel whose blocks were not all resident ends with an
+// error status instead of spinning. `extra` > 0 makes the barrier wait for that many arrivals
+// beyond the grid, which never come: every block's wait runs out (the host's test of this path).
 constexpr unsigned long long kBarrierNs = 1000000000ull;  // 1 s
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
@@ -144,21 +146,23 @@ __device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
   asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* err) {
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* err,
+                                             unsigned long long limit_ns = kBarrierNs,
+                                             unsigned extra = 0) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     ok = 1;
     const unsigned gen = ld_acquire_u32(&bar[1]);  // cannot advance before this block arrives
     __threadfence();
-    if (atomicAdd(&bar[0], 1u) == gridDim.x - 1) {
+    if (atomicAdd(&bar[0], 1u) == gridDim.x - 1 + extra) {
       atomicExch(&bar[0], 0u);
       __threadfence();
       atomicAdd(&bar[1], 1u);
     } else {
       const unsigned long long t0 = global_ns();
       while (ld_acquire_u32(&bar[1]) == gen) {
-        if (global_ns() - t0 > kBarrierNs) {
+        if (global_ns() - t0 > limit_ns) {
           atomicOr(err, ERRF_BARRIER);
           ok = 0;
           break;

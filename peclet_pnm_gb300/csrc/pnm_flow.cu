@@ -683,6 +683,7 @@ inline int fixed_scale(double bound) {
 
 Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const float spacing[3],
                         const FlowInputs& in, FlowOutputsDev* out) {
+  StageScope stage(c, PNM_STAGE_NETWORK_FLOW, "nf::network_flow");
   cudaStream_t s = c.stream;
   const Dims d = st.d;
   const long long n = d.n();

@@ -6,7 +6,7 @@
 // and long-running serving loops that must not enter the driver allocator while other work is
 // in flight (cudaMalloc / cudaFree can implicitly synchronise the device). Such a caller passes
 // its device input and output buffers and a stream; the only scratch this entry point uses is
-// the file-scope device array below, reserved when the library is loaded.
+// the file-scope device array below.
 //
 // Limits and sharing:
 //  * at most kNoAllocMaxVoxels voxels per call; larger volumes are rejected with
@@ -17,7 +17,11 @@
 //    different streams, or host threads racing — corrupt each other's results. Serialise calls
 //    per device (one stream, or an event between calls);
 //  * the first call on each device looks up the array's device address (cudaGetSymbolAddress,
-//    with that device current) and caches it; make that first call before any stream capture.
+//    with that device current) and caches it. Under CUDA's lazy module loading (the default
+//    since CUDA 12.2) that first call is also when the driver loads this library's kernels on
+//    the device and reserves the array, which allocates and may synchronise: make the first call
+//    at start-up, before the caller's pool claims the device's memory and before any stream
+//    capture (or set CUDA_MODULE_LOADING=EAGER, which loads the module with the context).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -71,7 +75,9 @@ constexpr int NX = 32, NY = 8, NZ = 8;
 
 // The peak test of the SDF pass on its own (pore_extraction.hpp:85-106): a voxel with
 // !(sdf <= 0) is a pore when no periodic neighbour has a larger (value, wrapped index). Bits go
-// into the caller-supplied bitmap (here: the static scratch array).
+// into the caller-supplied bitmap (here: the static scratch array). One block per 32 x 8 x 8
+// tile on a 1-D grid (tile = (bz * tny + by) * tnx + bx), so no shape meets the 65,535 limit of
+// a grid's y and z extents.
 __global__ void __launch_bounds__(NX* NY)
     k_peak_bits(const float* __restrict__ sdf, Dims d, uint32_t* __restrict__ bits) {
   constexpr int HX = NX + 2, HY = NY + 2, HZ = NZ + 2, NT = NX * NY;
@@ -79,7 +85,9 @@ __global__ void __launch_bounds__(NX* NY)
   __shared__ int wx[HX], wy[HY], wz[HZ];
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int nxy = nx * ny;
-  const int X0 = blockIdx.x * NX, Y0 = blockIdx.y * NY, Z0 = blockIdx.z * NZ;
+  const int tnx = (nx + NX - 1) / NX, tny = (ny + NY - 1) / NY;
+  const int tile = (int)blockIdx.x;
+  const int X0 = (tile % tnx) * NX, Y0 = ((tile / tnx) % tny) * NY, Z0 = (tile / tnx / tny) * NZ;
   const int t = threadIdx.x;
   if (t < HX) wx[t] = ((X0 - 1 + t) % nx + nx) % nx;
   if (t < HY) wy[t] = ((Y0 - 1 + t) % ny + ny) % ny;
@@ -142,14 +150,18 @@ extern "C" int pnm_extract_pores_noalloc(const float* d_sdf, int32_t nx, int32_t
     cudaGetLastError();
     return PNM_ERR_CUDA;
   }
-  const dim3 grid((unsigned)((nx + NX - 1) / NX), (unsigned)((ny + NY - 1) / NY),
-                  (unsigned)((nz + NZ - 1) / NZ));
-  k_peak_bits<<<grid, NX * NY, 0, s>>>(d_sdf, d, bits);
+  // tiles <= 2^26 / 1 (a 1 x 1 x 2^26 volume): within a 1-D grid's 2^31 - 1 blocks
+  const long long tiles = (long long)((nx + NX - 1) / NX) * ((ny + NY - 1) / NY) *
+                          ((nz + NZ - 1) / NZ);
+  k_peak_bits<<<(unsigned)tiles, NX * NY, 0, s>>>(d_sdf, d, bits);
+  if (cudaGetLastError() != cudaSuccess) return PNM_ERR_CUDA;
   long long launches = 0;
   exclusive_scan(PopcountOf{bits}, words, pref, part, s, &launches);
+  if (cudaGetLastError() != cudaSuccess) return PNM_ERR_CUDA;
   const unsigned egrid = (unsigned)std::min<long long>((words + 255) / 256, 152 * 8);
   const long long cap = std::min<long long>(pore_cap, 1000000);  // max_pores, :77
   launch_pores_emit(d_sdf, d, bits, pref, words, origin_xyz, spacing_xyz, d_pores, cap, egrid, s);
+  if (cudaGetLastError() != cudaSuccess) return PNM_ERR_CUDA;
   unsigned total = 0;
   if (cudaMemcpyAsync(&total, pref + words, sizeof(unsigned), cudaMemcpyDeviceToHost, s) !=
           cudaSuccess ||

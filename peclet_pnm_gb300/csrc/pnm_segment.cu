@@ -589,7 +589,8 @@ __global__ void __launch_bounds__(256)
 template <class G>
 __global__ void __launch_bounds__(256)
     k_flood_loop(G geo, const uint8_t* __restrict__ code, int* key, int* L, int* fa, int* fb,
-                 int* tmp, unsigned* cnt, int max_sweeps) {
+                 int* tmp, unsigned* cnt, int max_sweeps, unsigned long long wait_ns,
+                 unsigned wait_extra) {
   unsigned* err = &cnt[CNT_ERR];
   unsigned* bar = &cnt[CNT_BAR0];
   int* fin = fa;
@@ -615,10 +616,10 @@ __global__ void __launch_bounds__(256)
     for (long long i = tid; i < nin; i += stride)
       tmp[i] = flood_assign_one<true>(geo, key, __ldcg(&fin[i]));
     if (tid == 0) atomicExch(&cnt[cout], 0u);  // read by nobody since the last barrier
-    if (!grid_barrier(bar, err)) break;
+    if (!grid_barrier(bar, err, wait_ns, wait_extra)) break;
     for (long long i = tid; i < nin; i += stride)
       flood_discover_one(geo, code, key, L, __ldcg(&fin[i]), __ldcg(&tmp[i]), fout, &cnt[cout]);
-    if (!grid_barrier(bar, err)) break;
+    if (!grid_barrier(bar, err, wait_ns, wait_extra)) break;
     int* t = fin;
     fin = fout;
     fout = t;
@@ -633,14 +634,28 @@ __global__ void __launch_bounds__(256)
 // ---- 5. first-appearance renumbering (pore_extraction.hpp:319-382) --------------------------------
 // Label ids are ranks of each label's minimum voxel id: flag those minima in two bitmaps (pore /
 // solid), prefix-count the bitmaps, and write the signed id back into L[key].
+// A key voxel k and its label minimum m = L[k] are voxel ids below n_vox whenever the stages
+// before ran to completion; an id outside [0, n_vox) (an upstream stage that stopped early) sets
+// ERRF_LABEL_RANGE and is skipped instead of indexing the bitmaps with it.
+__device__ __forceinline__ bool key_in_range(int k, int m, long long n_vox, unsigned* err) {
+  if (k >= 0 && k < n_vox && m >= 0 && m < n_vox) return true;
+  atomicOr(err, ERRF_LABEL_RANGE);
+  return false;
+}
+
 __global__ void k_key_first(const int* __restrict__ keylist, const unsigned* nkeys_p,
                             const int* __restrict__ L, const uint8_t* __restrict__ code,
-                            uint32_t* firstP, uint32_t* firstS) {
+                            uint32_t* firstP, uint32_t* firstS, long long n_vox, unsigned* err) {
   const unsigned nk = *nkeys_p;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nk;
        i += (long long)gridDim.x * blockDim.x) {
     const int k = keylist[i];
+    if (k < 0 || k >= n_vox) {
+      atomicOr(err, ERRF_LABEL_RANGE);
+      continue;
+    }
     const int m = L[k];
+    if (!key_in_range(k, m, n_vox, err)) continue;
     uint32_t* bits = code_cls(code[k]) == CLS_PORE ? firstP : firstS;
     atomicOr(&bits[m >> 5], 1u << (m & 31));
   }
@@ -649,12 +664,18 @@ __global__ void k_key_first(const int* __restrict__ keylist, const unsigned* nke
 template <class G>
 __global__ void k_key_id(G geo, const int* __restrict__ keylist, const unsigned* nkeys_p, int* L,
                          const uint8_t* __restrict__ code, const uint32_t* firstP,
-                         const unsigned* prefP, const uint32_t* firstS, const unsigned* prefS) {
+                         const unsigned* prefP, const uint32_t* firstS, const unsigned* prefS,
+                         long long n_vox, unsigned* err) {
   const unsigned nk = *nkeys_p;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nk;
        i += (long long)gridDim.x * blockDim.x) {
     const int k = keylist[i];
+    if (k < 0 || k >= n_vox) {
+      atomicOr(err, ERRF_LABEL_RANGE);
+      continue;
+    }
     const int m = L[k];
+    if (!key_in_range(k, m, n_vox, err)) continue;
     int off, nx, ny, nz;  // ranks count from the volume's first voxel (a word boundary)
     geo.locate(k, off, nx, ny, nz);
     L[k] = code_cls(code[k]) == CLS_PORE
@@ -1053,13 +1074,14 @@ inline float marker_threshold(const float spacing[3]) {
 template <class G>
 cudaError_t launch_flood_loop(G geo, const uint8_t* code, int* key, int* L, int* fa, int* fb,
                               int* tmp, unsigned* cnt, int max_sweeps, int sm_count,
-                              long long work, cudaStream_t s, int blocks_per_sm = 2) {
+                              long long work, cudaStream_t s, int blocks_per_sm = 2,
+                              unsigned long long wait_ns = kBarrierNs, unsigned wait_extra = 0) {
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_flood_loop<G>, 256, 0);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorCooperativeLaunchTooLarge;
   const unsigned grid = grid_for(work, 256, sm_count, std::min(per_sm, blocks_per_sm));
-  void* args[] = {&geo, &code, &key, &L, &fa, &fb, &tmp, &cnt, &max_sweeps};
+  void* args[] = {&geo, &code, &key, &L, &fa, &fb, &tmp, &cnt, &max_sweeps, &wait_ns, &wait_extra};
   return cudaLaunchCooperativeKernel((const void*)k_flood_loop<G>, dim3(grid), dim3(256), args, 0,
                                      s);
 }
@@ -1074,6 +1096,7 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
                     bool all_ascent, HostXfer* xfer) {
   const long long n = d.n();
   const long long words = (n + 31) / 32;
+  StageScope stage(c, PNM_STAGE_SDF_PASS, "pnm::extract_pores+init_markers");
   st->d = d;
   st->sdf = d_sdf;
   PNM_TRY(c.buf(S_CODE, n, &st->code));
@@ -1153,22 +1176,32 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   st->key = key;
   const unsigned tiles = (unsigned)boxes_of(d, TX, TY, TZ_PLAIN);
 
-  k_ccl_words<<<grid_for(st->n_words, 256, c.sm_count, PLAIN_GRID_PER_SM), 256, 0, s>>>(
-      geo, st->mbits, st->n_words, L, c.d_cnt);
-  k_resolve<<<(unsigned)boxes_of(d, RTX, RTY, RTZ), RTX * RTY, 0, s>>>(geo, st->code, st->nxt, L,
-                                                                      key, keylist, c.d_cnt);
+  {
+    StageScope stage(c, PNM_STAGE_MERGE_MARKERS, "pnm::merge_markers");
+    k_ccl_words<<<grid_for(st->n_words, 256, c.sm_count, PLAIN_GRID_PER_SM), 256, 0, s>>>(
+        geo, st->mbits, st->n_words, L, c.d_cnt);
+    ++c.launches;
+  }
+  {
+    StageScope stage(c, PNM_STAGE_GRADIENT_PATH, "pnm::gradient_path");
+    k_resolve<<<(unsigned)boxes_of(d, RTX, RTY, RTZ), RTX * RTY, 0, s>>>(geo, st->code, st->nxt,
+                                                                        L, key, keylist, c.d_cnt);
+    ++c.launches;
+  }
+  StageScope flood_stage(c, PNM_STAGE_FLOOD, "pnm::flood");
   k_flood_seed<OneVol, TZ_PLAIN><<<tiles, TX * TY, 0, s>>>(geo, st->code, key, L, ulist, c.d_cnt);
   const unsigned fgrid = grid_for(n, 256, c.sm_count, 4);
   k_flood_layer2<<<fgrid, 256, 0, s>>>(geo, st->code, key, ulist, &c.d_cnt[CNT_ULIST], f0,
                                        &c.d_cnt[CNT_FRONT0]);
-  c.launches += 4;
+  c.launches += 2;
   PNM_CUDA(cudaGetLastError());
 
   // deeper layers: the persistent loop; if a cooperative launch is refused, the same sweeps as
   // separate launches in batches between host checks (empty sweeps are no-ops)
   const int kMaxSweeps = 1 << 20;
   cudaError_t le = launch_flood_loop(geo, st->code, key, L, f0, f1, tmp, c.d_cnt, kMaxSweeps,
-                                     c.sm_count, n, s, PLAIN_FLOOD_PER_SM);
+                                     c.sm_count, n, s, PLAIN_FLOOD_PER_SM, c.wait_ns,
+                                     c.wait_extra);
   ++c.launches;
   if (le != cudaSuccess) {
     cudaGetLastError();
@@ -1195,8 +1228,7 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
     }
     st->flood_sweeps = sweeps;
   }
-
-  // renumbering
+  flood_stage.next(PNM_STAGE_RELABEL, "pnm::relabel");
   uint32_t *firstP, *firstS;
   unsigned *prefP, *prefS, *scan0;
   PNM_TRY(c.buf(S_FIRSTP, words, &firstP));
@@ -1207,11 +1239,12 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   PNM_CUDA(cudaMemsetAsync(firstP, 0, words * 4, s));
   PNM_CUDA(cudaMemsetAsync(firstS, 0, words * 4, s));
   const unsigned kgrid = grid_for(n / 16 + 1, 256, c.sm_count);  // grid-stride over the keys
-  k_key_first<<<kgrid, 256, 0, s>>>(keylist, &c.d_cnt[CNT_KEYS], L, st->code, firstP, firstS);
+  k_key_first<<<kgrid, 256, 0, s>>>(keylist, &c.d_cnt[CNT_KEYS], L, st->code, firstP, firstS, n,
+                                    &c.d_cnt[CNT_ERR]);
   exclusive_scan(PopcountOf{firstP}, words, prefP, scan0, s, &c.launches);
   exclusive_scan(PopcountOf{firstS}, words, prefS, scan0, s, &c.launches);
   k_key_id<<<kgrid, 256, 0, s>>>(geo, keylist, &c.d_cnt[CNT_KEYS], L, st->code, firstP, prefP,
-                                 firstS, prefS);
+                                 firstS, prefS, n, &c.d_cnt[CNT_ERR]);
   c.launches += 2;
   PNM_CUDA(cudaGetLastError());
   unsigned tot[2];
@@ -1227,7 +1260,10 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   if (c.h_cnt[CNT_ERR] & ERRF_FLOOD_LIMIT)
     return Status{PNM_ERR_NOT_CONVERGED, "flood did not converge"};
   if (c.h_cnt[CNT_ERR] & ERRF_BARRIER)
-    return Status{PNM_ERR_INTERNAL, "persistent flood loop: grid barrier timed out"};
+    return Status{PNM_ERR_NOT_CONVERGED,
+                  "flood loop: a grid barrier wait ran out (blocks not all resident?)"};
+  if (c.h_cnt[CNT_ERR] & ERRF_LABEL_RANGE)
+    return Status{PNM_ERR_INTERNAL, "renumbering: a label minimum is outside the volume"};
   return Status::ok();
 }
 
@@ -1240,6 +1276,7 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
   long long cap = 4096;
   while (cap < cap_hint) cap <<= 1;
   for (int attempt = 0; attempt < 8; ++attempt) {
+    StageScope stage(c, PNM_STAGE_SEG_PAIRS, "pnm::relabel_seg+boundary_pairs");
     unsigned long long* table = nullptr;
     int* range = nullptr;
     PNM_TRY(c.buf(S_HASH, want_pairs ? cap : 1, &table));
@@ -1291,6 +1328,7 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
       cap <<= 2;
       continue;
     }
+    stage.next(PNM_STAGE_PAIR_SORT, "pnm::unique_pairs");
     const long long m = c.h_cnt[CNT_PAIRS];
     *n_pairs = m;
     int32_t* out = nullptr;
@@ -1337,6 +1375,7 @@ Status run_topology_of_seg(Ctx& c, const int32_t* d_seg, Dims d, int32_t** d_pai
 
 Status run_pores(Ctx& c, const SegState& st, const float origin[3], const float spacing[3],
                  pnm_pore* d_out, int64_t cap, int64_t* n_pores) {
+  StageScope stage(c, PNM_STAGE_PORES, "pnm::extract_pores(records)");
   cudaStream_t s = c.stream;
   const long long words = (st.d.n() + 31) / 32;
   unsigned *pref, *scan0;
@@ -1399,11 +1438,12 @@ Status enqueue_batch(BatchPlan& p, cudaStream_t s, long long* launches) {
   PNM_CUDA(launch_flood_loop(geo, p.code, p.key, p.L, p.f0, p.f1, p.tmp, p.cnt, p.max_sweeps, sm,
                              n, s, p.flood_blocks_per_sm));
   const unsigned kgrid = grid_for(n / 16 + 1, 256, sm, p.grid_per_sm);
-  k_key_first<<<kgrid, 256, 0, s>>>(p.keylist, &p.cnt[CNT_KEYS], p.L, p.code, p.firstP, p.firstS);
+  k_key_first<<<kgrid, 256, 0, s>>>(p.keylist, &p.cnt[CNT_KEYS], p.L, p.code, p.firstP, p.firstS,
+                                    n, &p.cnt[CNT_ERR]);
   exclusive_scan(PopcountOf{p.firstP}, words, p.prefP, p.scan_tmp, s, launches);
   exclusive_scan(PopcountOf{p.firstS}, words, p.prefS, p.scan_tmp, s, launches);
   k_key_id<<<kgrid, 256, 0, s>>>(geo, p.keylist, &p.cnt[CNT_KEYS], p.L, p.code, p.firstP,
-                                 p.prefP, p.firstS, p.prefS);
+                                 p.prefP, p.firstS, p.prefS, n, &p.cnt[CNT_ERR]);
   k_batch_labels<<<1, SCAN_THREADS, 0, s>>>(p.vols, p.res, p.nvol, p.prefP, p.prefS);
   k_seg_topo<<<(unsigned)p.bricks, STX * STY, 0, s>>>(geo, KeyLabels{p.key, p.L}, p.seg, 1,
                                                        p.table, (uint64_t)(p.hash_cap - 1), p.cnt,

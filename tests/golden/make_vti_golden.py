@@ -8,7 +8,7 @@ WholeExtent is one larger than the arrays). Each case stores the file bytes and 
 returned. Writer: scripts/vti.py save_vti is imported from the reference checkout and its output
 for a small labelled volume is stored byte for byte.
 
-    python tests/golden/make_vti_golden.py
+    PNM_REFERENCE=<reference checkout> python tests/golden/make_vti_golden.py
 """
 from __future__ import annotations
 
@@ -22,7 +22,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("PNM_REFERENCE", "/root/reference")
+REF = os.environ.get("PNM_REFERENCE", "")  # the reference checkout (read-only)
 
 HEAD = (b'<?xml version="1.0"?>\n<VTKFile type="ImageData" version="1.0" '
         b'byte_order="LittleEndian" header_type="UInt64">\n')
@@ -79,6 +79,9 @@ def writer_case(rng, mod) -> bytes:
 
 
 def main():
+    if not os.path.exists(os.path.join(REF, "scripts", "vti.py")):
+        sys.stderr.write("set PNM_REFERENCE to the reference checkout\n")
+        return 2
     lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libpnm_ref_vti.so"))
     lib.ref_read_vti.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p,
                                  ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),

@@ -43,6 +43,23 @@ def test_null_context_is_rejected():
                                    _capi.as_ptr(s), ctypes.byref(pp), ctypes.byref(n)) == \
         _capi.PNM_ERR_ARG
     assert _capi.pnm_ctx_set_stream(None, None) == _capi.PNM_ERR_ARG
+    assert _capi.pnm_ctx_set_timing(None, 1) == _capi.PNM_ERR_ARG
+    assert _capi.pnm_ctx_set_wait_limit(None, 1000, 0) == _capi.PNM_ERR_ARG
+
+
+def test_stats_struct_matches_header():
+    """pnm_stats in the header ends with stage_ms[PNM_STAGE_COUNT]; the ctypes mirror has the
+    same stage count and names every PNM_STAGE_* in order."""
+    from peclet_pnm_gb300 import _capi
+
+    text = open(HEADER).read()
+    count = int(re.search(r"#define PNM_STAGE_COUNT (\d+)", text).group(1))
+    stages = re.findall(r"#define PNM_STAGE_([A-Z_]+) (\d+)", text)
+    ids = {name: int(v) for name, v in stages if name != "COUNT"}
+    assert sorted(ids.values()) == list(range(count)) == list(range(len(_capi.STAGES)))
+    for name, i in ids.items():
+        assert _capi.STAGES[i] == name.lower()
+    assert _capi.PnmStats.stage_ms.size == count * 8
 
 
 def test_no_cpu_fallback_without_device():

@@ -22,18 +22,23 @@ def _regular(pnm, sdf):
     return pnm.pores_array(sdf, [0.0, 0.0, 0.0], [1.0, 1.0, 1.0])
 
 
-def _noalloc(capi, torch, sdf, cap=200000):
-    d_sdf = torch.from_numpy(np.ascontiguousarray(sdf, np.float32)).cuda()
-    d_out = torch.empty((cap, 4), dtype=torch.float32, device="cuda")
+def _noalloc(capi, torch, sdf, cap=200000, rows=None, stream=None):
+    """Runs the entry point on `stream` (default: torch's current stream) into an output of
+    `rows` records (default: cap) filled with a canary value; returns (rc, output, count)."""
+    rows = cap if rows is None else rows
+    st = stream if stream is not None else torch.cuda.current_stream()
+    with torch.cuda.stream(st):
+        d_sdf = torch.from_numpy(np.ascontiguousarray(sdf, np.float32)).cuda()
+        d_out = torch.full((rows, 4), -7.5, dtype=torch.float32, device="cuda")
     nz, ny, nx = sdf.shape
     o = np.zeros(3, np.float32)
     s = np.ones(3, np.float32)
     n = capi._i64()
-    stream = torch.cuda.current_stream().cuda_stream
     rc = capi.pnm_extract_pores_noalloc(d_sdf.data_ptr(), nx, ny, nz, capi.as_ptr(o),
                                         capi.as_ptr(s), d_out.data_ptr(), cap, ctypes.byref(n),
-                                        stream)
-    return rc, d_out[: n.value].cpu().numpy(), n.value
+                                        st.cuda_stream)
+    st.synchronize()
+    return rc, d_out.cpu().numpy(), n.value
 
 
 def test_noalloc_matches_regular_entry_point_twice():
@@ -48,7 +53,28 @@ def test_noalloc_matches_regular_entry_point_twice():
         assert rc == _capi.PNM_OK
         want = _regular(pnm, sdf)
         assert n == len(want)
-        assert np.array_equal(got.view(np.int32), want.view(np.int32))  # same voxel order, bitwise
+        # same voxel order, bitwise
+        assert np.array_equal(got[:n].view(np.int32), want.view(np.int32))
+
+
+def test_noalloc_capacity_and_side_stream():
+    """pore_cap below the count: PNM_ERR_CAPACITY, the full count reported, only the first
+    pore_cap records written; then a call on a fresh (non-default) stream."""
+    torch = pytest.importorskip("torch")
+    import peclet_pnm_gb300 as pnm
+    from peclet_pnm_gb300 import _capi
+
+    sdf = syn.packing((72, 80, 96), 0.4, seed=51)
+    want = _regular(pnm, sdf)
+    assert len(want) > 3
+    rc, got, n = _noalloc(_capi, torch, sdf, cap=3, rows=8)
+    assert rc == _capi.PNM_ERR_CAPACITY and n == len(want)
+    assert np.array_equal(got[:3].view(np.int32), want[:3].view(np.int32))
+    assert np.all(got[3:] == np.float32(-7.5)), "records past pore_cap were written"
+    side = torch.cuda.Stream()
+    rc, got, n = _noalloc(_capi, torch, sdf, stream=side)
+    assert rc == _capi.PNM_OK and n == len(want)
+    assert np.array_equal(got[:n].view(np.int32), want.view(np.int32))
 
 
 def test_noalloc_rejects_volumes_beyond_its_scratch():
