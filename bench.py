@@ -59,6 +59,9 @@ def parse():
                     help="skip the Poisson serving measurement")
     ap.add_argument("--no-flow", action="store_true",
                     help="skip the 256^3 float64 extract_network_flow measurement")
+    ap.add_argument("--profile", choices=["plain", "flow"], default=None,
+                    help="run one call of a leg inside an NVTX range named 'profiled_call' "
+                         "(after warm-up calls) and exit: the target of an ncu launch list")
     ap.add_argument("--batch-volumes", type=int, default=96)
     ap.add_argument("--serve-requests", type=int, default=600)
     return ap.parse_args()
@@ -349,23 +352,35 @@ def batched_bench(args, dev):
     return out
 
 
+FLOW_BYTES_PER_VOXEL = 164  # extract_network_flow algorithmic bytes per voxel (60 + 104)
+
+
+def flow_inputs(dev, n=256):
+    """The 256^3 float64 packing (seed 3) and its Fourier fields (seed 4), on the device."""
+    from peclet_pnm_gb300 import synthetic as syn
+
+    sdf = syn.packing((n, n, n), 0.4, seed=3, dtype=np.float64, device=dev)
+    return sdf, syn.fourier_fields_device(sdf)
+
+
 def flow_bench(args, dev):
     """extract_network_flow on a 256^3 float64 packing (seed 3) with u, v, w, p = 32 random Fourier
     modes (|k| <= 8, amplitude 1e-3, seed 4) zeroed in solid, openness clamp(0.5 + face SDF, 0, 1),
-    grad_p_zyx = [0, 0, -1e-4]; through the host C ABI (host SDF and fields in, host results out,
-    the reference binding's call). Check: the pore residuals of a closed periodic network sum to
-    zero (every throat flux leaves one pore and enters another). `device`: the same call on
-    device-resident inputs (pnm_extract_network_flow_dev, a solver's fields handed over in place),
-    timed with CUDA events on the context's stream."""
+    grad_p_zyx = [0, 0, -1e-4].
+
+    `device`: pnm_extract_network_flow_dev on device-resident inputs (a solver's fields handed over
+    in place), CUDA events on the context's stream; its roofline is the 164 B/voxel model against
+    the measured HBM peak. `e2e`: the host C ABI call (host SDF and fields in, host results out,
+    the reference binding's call). `h2d`: the pinned host-to-device copy of the same 1.07 GB of
+    inputs alone, which bounds the host call from below. Check: the pore residuals of a closed
+    periodic network sum to zero. `cpu_baseline`: the oracle port on all host cores, one call."""
     import torch
 
     import peclet_pnm_gb300 as pnm
     from peclet_pnm_gb300 import _capi
-    from peclet_pnm_gb300 import synthetic as syn
 
     n = 256
-    sdf = syn.packing((n, n, n), 0.4, seed=3, dtype=np.float64, device=dev)
-    fields = syn.fourier_fields_device(sdf)
+    sdf, fields = flow_inputs(dev, n)
     o = np.zeros(3, np.float32)
     s = np.ones(3, np.float32)
     g = np.array([0.0, 0.0, -1e-4], np.float64)[::-1].copy()  # xyz
@@ -385,7 +400,7 @@ def flow_bench(args, dev):
     for _ in range(3):
         call_dev()
     stream.synchronize()
-    reps = 5
+    reps = 10
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(reps):
@@ -394,16 +409,35 @@ def flow_bench(args, dev):
     e1.synchronize()
     t_dev = e0.elapsed_time(e1) / 1e3 / reps
     dev_counts = (int(rd.n_pores), int(rd.n_throats))
+    ctx.set_timing(True)
+    call_dev()
+    stage_ms = ctx.stats()["stage_ms"]
+    ctx.set_timing(False)
     ctx.set_stream(None)
-    del d_sdf, d_f
+    # pinned host copies of the inputs; the H2D of all of them alone, for scale
     h_sdf = torch.empty((n, n, n), dtype=torch.float32, pin_memory=True)
-    h_sdf.copy_(sdf.to(torch.float32))
+    h_sdf.copy_(d_sdf)
     hf = []
     for f in fields:
         h = torch.empty((n, n, n), dtype=torch.float64, pin_memory=True)
         h.copy_(f)
         hf.append(h)
-    del sdf, fields
+    h2d_bytes = 4 * n ** 3 + 7 * 8 * n ** 3
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            d_sdf.copy_(h_sdf, non_blocking=True)
+            for h, d in zip(hf, d_f):
+                d.copy_(h, non_blocking=True)
+        e0.record(stream)
+        d_sdf.copy_(h_sdf, non_blocking=True)
+        for h, d in zip(hf, d_f):
+            d.copy_(h, non_blocking=True)
+        e1.record(stream)
+    e1.synchronize()
+    t_h2d = e0.elapsed_time(e1) / 1e3
+    sdf_np = sdf.cpu().numpy()
+    fields_np = None if args.no_cpu_baseline else [f.cpu().numpy() for f in fields]
+    del sdf, fields, d_sdf, d_f
     torch.cuda.empty_cache()
     res = _capi._P(_capi.PnmFlowResult)()
 
@@ -416,7 +450,7 @@ def flow_bench(args, dev):
         call()
         _capi.pnm_flow_result_free(res)
     ts = []
-    for _ in range(3):
+    for _ in range(5):
         t0 = time.perf_counter()
         call()
         ts.append(time.perf_counter() - t0)
@@ -428,15 +462,92 @@ def flow_bench(args, dev):
     t = float(np.median(ts))
     scale = float(np.abs(flow).sum()) or 1.0
     ctx.close()
-    return {"workload": "extract_network_flow 256^3 float64 packing (seed 3), 32-mode Fourier "
-                        "u,v,w,p (seed 4), openness from face SDF, grad_p_zyx [0,0,-1e-4]",
-            "e2e": {"value": n ** 3 / t / 1e9, "unit": "Gvoxel/s", "ms_per_step": t * 1e3,
-                    "h2d_bytes_per_step": 4 * n ** 3 + 7 * 8 * n ** 3},
-            "device": {"value": n ** 3 / t_dev / 1e9, "unit": "Gvoxel/s",
-                       "ms_per_step": t_dev * 1e3, "h2d_bytes_per_step": 0,
-                       "same_counts": dev_counts == (npo, nth)},
-            "pores": npo, "throats": nth,
-            "residual_sum_over_flux": float(abs(resid.sum())) / scale}
+    peak, peak_src = measured_hbm_peak()
+    achieved = FLOW_BYTES_PER_VOXEL * n ** 3 / t_dev / 1e9
+    out = {"workload": "extract_network_flow 256^3 float64 packing (seed 3), 32-mode Fourier "
+                       "u,v,w,p (seed 4), openness from face SDF, grad_p_zyx [0,0,-1e-4]",
+           "device": {"value": n ** 3 / t_dev / 1e9, "unit": "Gvoxel/s",
+                      "ms_per_step": t_dev * 1e3, "h2d_bytes_per_step": 0,
+                      "same_counts": dev_counts == (npo, nth),
+                      "stage_ms": {k: round(v, 4) for k, v in stage_ms.items() if v > 0}},
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "model_bytes_per_voxel": FLOW_BYTES_PER_VOXEL,
+                        "kernel": "extract_network_flow device pipeline (all kernels of one "
+                                  "call, SDF and fields resident)",
+                        "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"},
+           "e2e": {"value": n ** 3 / t / 1e9, "unit": "Gvoxel/s", "ms_per_step": t * 1e3,
+                   "ms_min": min(ts) * 1e3, "h2d_bytes_per_step": h2d_bytes,
+                   "d2h_bytes_per_step": 16 * npo + 16 * npo + nth * (8 + 24)},
+           "h2d": {"ms": t_h2d * 1e3, "gb_per_s": h2d_bytes / t_h2d / 1e9,
+                   "what": "pinned H2D of the SDF and the seven float64 fields alone"},
+           "pores": npo, "throats": nth,
+           "residual_sum_over_flux": float(abs(resid.sum())) / scale}
+    if fields_np is not None:
+        from oracle import Oracle
+
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        Oracle("port", threads=threads).extract_network_flow(
+            sdf_np, [0.0] * 3, [1.0] * 3, *fields_np[:4], ox=fields_np[4], oy=fields_np[5],
+            oz=fields_np[6], grad_p_zyx=[0.0, 0.0, -1e-4])
+        t_cpu = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n ** 3 / t_cpu / 1e9, "unit": "Gvoxel/s",
+                               "cores": threads, "kind": "port",
+                               "sample": f"the whole 256^3 flow workload, one call ({t_cpu:.1f} s,"
+                                         " the project's C++ restatement, OpenMP)"}
+    return out
+
+
+def profile_call(args, dev):
+    """Warm-up calls of one leg, then one call inside the NVTX range 'profiled_call' (ncu:
+    --nvtx --nvtx-include "profiled_call/"); prints the call's figures."""
+    import torch
+
+    import peclet_pnm_gb300 as pnm
+    from peclet_pnm_gb300 import _capi
+
+    ctx = pnm.Context(dev.index)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    o = np.zeros(3, np.float32)
+    s = np.ones(3, np.float32)
+    if args.profile == "flow":
+        n = 256
+        sdf, fields = flow_inputs(dev, n)
+        d_sdf = sdf.to(torch.float32).contiguous()
+        del sdf
+        g = np.array([-1e-4, 0.0, 0.0], np.float64)
+        rd = _capi.PnmFlowResultDev()
+
+        def call():
+            ctx.check(_capi.pnm_extract_network_flow_dev(
+                ctx.h, ctypes.c_void_p(d_sdf.data_ptr()), n, n, n, _capi.as_ptr(o),
+                _capi.as_ptr(s), *[ctypes.c_void_p(f.data_ptr()) for f in fields],
+                _capi.as_ptr(g), ctypes.byref(rd)))
+    else:
+        n = args.size
+        sdf = gen_volume(n, replica_seed(0), dev)
+        d_seg = torch.empty(sdf.numel(), dtype=torch.int32, device=dev)
+        d_pores = torch.empty((1_000_000, 4), dtype=torch.float32, device=dev)
+        d_pairs = torch.empty((4_000_000, 2), dtype=torch.int32, device=dev)
+        npo, npa = _capi._i64(), _capi._i64()
+
+        def call():
+            ctx.check(_capi.pnm_extract_pore_network_dev(
+                ctx.h, sdf.data_ptr(), n, n, n, _capi.as_ptr(o), _capi.as_ptr(s),
+                d_pores.data_ptr(), 1_000_000, ctypes.byref(npo), d_seg.data_ptr(),
+                d_pairs.data_ptr(), 4_000_000, ctypes.byref(npa)))
+    for _ in range(max(1, args.warmup)):
+        call()
+    torch.cuda.synchronize(dev)
+    l0 = ctx.stats()["launches"]
+    torch.cuda.nvtx.range_push("profiled_call")
+    call()
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize(dev)
+    print(json.dumps({"profile": args.profile, "edge": n,
+                      "launches": ctx.stats()["launches"] - l0}), flush=True)
+    ctx.close()
 
 
 def served_bench(args, dev):
@@ -630,6 +741,11 @@ def ours(args, rank, world, local_rank):
     launches = ctx.stats()["launches"] - launches0
     ms = e0.elapsed_time(e1) / args.steps
     st = ctx.stats()
+    # one more call outside the timed region with per-stage device timing on
+    ctx.set_timing(True)
+    step()
+    stage_ms = ctx.stats()["stage_ms"]
+    ctx.set_timing(False)
     s_max, value = whole_job_rate(ms * 1e-3, nvox, world, dev)
     ms_max = s_max * 1e3
 
@@ -678,6 +794,7 @@ def ours(args, rank, world, local_rank):
                 "h2d_bytes_per_step": 4 * nvox,
                 "d2h_bytes_per_step": 4 * nvox + 16 * int(npp.value) + 8 * int(npr.value)},
         "gpu_launches": launches,
+        "stage_ms": {k: round(v, 4) for k, v in stage_ms.items() if v > 0},
         "clocks": clk,
         "outputs": {"pores": int(st["n_pores"]), "pairs": int(st["n_pairs"]),
                     "pore_labels": int(st["n_pore_labels"]),
@@ -716,6 +833,12 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         reference_arm(args, rank)
+        return
+    if args.profile:
+        import torch
+
+        torch.cuda.set_device(local_rank)
+        profile_call(args, torch.device("cuda", local_rank))
         return
     if world > 1:
         import torch

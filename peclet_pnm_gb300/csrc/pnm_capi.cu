@@ -83,12 +83,10 @@ Status Ctx::read_counters() {
 void Ctx::call_begin() {
   for (double& t : last.stage_ms) t = 0.0;
   tstage.clear();
+  open_stages.clear();
 }
 
-void Ctx::stage_begin(int id, const char* name) {
-  nvtxRangePushA(name);
-  ++nvtx_depth;
-  if (!timing) return;
+void Ctx::interval_begin(int id) {
   const size_t k = tstage.size();
   while (tev.size() < 2 * k + 2) {
     cudaEvent_t e;
@@ -105,10 +103,25 @@ void Ctx::stage_begin(int id, const char* name) {
   tstage.push_back(id);
 }
 
+void Ctx::interval_end() {
+  if (tstage.empty()) return;
+  if (cudaEventRecord(tev[2 * (tstage.size() - 1) + 1], stream) != cudaSuccess) cudaGetLastError();
+}
+
+void Ctx::stage_begin(int id, const char* name) {
+  nvtxRangePushA(name);
+  ++nvtx_depth;
+  if (!timing) return;
+  if (!open_stages.empty()) interval_end();  // pause the enclosing stage
+  open_stages.push_back(id);
+  interval_begin(id);
+}
+
 void Ctx::stage_end() {
-  if (timing && !tstage.empty()) {
-    const size_t k = tstage.size() - 1;
-    if (cudaEventRecord(tev[2 * k + 1], stream) != cudaSuccess) cudaGetLastError();
+  if (timing && !open_stages.empty()) {
+    interval_end();
+    open_stages.pop_back();
+    if (!open_stages.empty()) interval_begin(open_stages.back());  // resume the enclosing one
   }
   if (nvtx_depth > 0) {
     nvtxRangePop();
@@ -132,6 +145,7 @@ void Ctx::stage_collect() {
       cudaGetLastError();
   }
   tstage.clear();
+  open_stages.clear();
 }
 
 Status check_dims(Dims d, const float* spacing, bool need_spacing) {

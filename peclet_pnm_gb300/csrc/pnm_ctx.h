@@ -102,10 +102,15 @@ struct Ctx {
   unsigned wait_extra = 0;
   // stages (PNM_STAGE_*): an NVTX range each, and with timing on a pair of CUDA events on the
   // stream around each, summed per stage into last.stage_ms when the call ends
+  // Stages nest (network flow runs a seg-only pass inside its own stage): an inner stage pauses
+  // the outer one, so the recorded intervals partition the call's device time.
   bool timing = false;
   std::vector<cudaEvent_t> tev;  // event pool, two per recorded stage interval
   std::vector<int> tstage;       // stage id of each recorded interval
+  std::vector<int> open_stages;  // stack of open stage ids
   int nvtx_depth = 0;
+  void interval_begin(int id);
+  void interval_end();
   void call_begin();                           // clears the last call's stage times
   void stage_begin(int id, const char* name);  // NVTX push (+ start event)
   void stage_end();                            // (end event +) NVTX pop

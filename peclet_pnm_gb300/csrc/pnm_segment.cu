@@ -54,6 +54,24 @@ __device__ __forceinline__ bool key_above(uint32_t o1, uint32_t p1, uint32_t o0,
   return (((uint64_t)o1 << 32) | p1) > (((uint64_t)o0 << 32) | p0);
 }
 
+// Candidate (0, 1, 2) = (c-1, c, c+1) of an axis holding the maximum (bits of `m`, at least
+// one set) with the largest wrapped coordinate. r: 0 no wrap (c+1 > c > c-1), 1 c == 0 (c-1
+// wraps to n-1: c-1 > c+1 > c), 2 c == n-1 (c+1 wraps to 0: c > c-1 > c+1). A table of 2-bit
+// answers indexed by (r, m).
+__device__ __forceinline__ int pick_ranked(unsigned m, int r) {
+  constexpr unsigned long long kLut =
+      // r = 0: 2 if bit 2, else 1 if bit 1, else 0
+      (0ull << 0) | (0ull << 2) | (1ull << 4) | (1ull << 6) | (2ull << 8) | (2ull << 10) |
+      (2ull << 12) | (2ull << 14) |
+      // r = 1: order 0, 2, 1
+      (0ull << 16) | (0ull << 18) | (1ull << 20) | (0ull << 22) | (2ull << 24) | (0ull << 26) |
+      (2ull << 28) | (0ull << 30) |
+      // r = 2: order 1, 0, 2
+      (0ull << 32) | (0ull << 34) | (1ull << 36) | (1ull << 38) | (2ull << 40) | (0ull << 42) |
+      (1ull << 44) | (1ull << 46);
+  return (int)((kLut >> (2 * (8 * r + m))) & 3ull);
+}
+
 template <bool ALL_ASCENT, class G, int TZ = 8>
 __global__ void __launch_bounds__(TX* TY, 8)  // 8 resident tiles per SM (32 registers)
     k_sdf_pass(const float* __restrict__ sdf, G geo, uint8_t* __restrict__ code,
@@ -108,6 +126,97 @@ __global__ void __launch_bounds__(TX* TY, 8)  // 8 resident tiles per SM (32 reg
   const int gx = X0 + tx, gy = Y0 + ty;
   const bool inxy = gx < nx && gy < ny;
   const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+  // Everything of an output voxel but its ascent direction: class, flood seed, code byte,
+  // marker run head and the chunk's marker word.
+  auto finish_voxel = [&](int tz, bool valid, int ci, int cls, int bk) {
+    const int gz = Z0 + tz;
+    // flood seed: a marker among the 26 neighbours (the voxel itself is no marker)
+    unsigned nb = 0;
+    if (__any_sync(0xffffffffu, valid && cls == CLS_FLOOD)) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) nb |= rowd[tz + k / 3][ty + k % 3];
+    }
+    if (valid) {
+      const bool seed = cls == CLS_FLOOD && ((nb >> lane) & 1u);
+      code[ci] = make_code(bk, cls, seed);
+    }
+    // marker runs of this chunk row
+    const unsigned m = rowm[tz + 1][ty + 1];
+    const bool marker = valid && ((m >> lane) & 1u);
+    const int hl = marker ? 31 - __clz((m & ~(m << 1)) & upto) : 0;
+    const int head = off + gz * nxy + gy * nx + X0 + hl;
+    if (valid) L[ci] = marker ? head : kBig;
+    if (lane == 0 && gy < ny && gz < nz) {
+      const int xe = nx - X0;  // valid x positions of this chunk
+      mbits[bx.word0 + (gz * ny + gy) * ((nx + 31) >> 5) + (X0 >> 5)] =
+          m & (xe >= 32 ? 0xffffffffu : ((1u << xe) - 1u));
+    }
+  };
+  auto voxel_class = [&](uint32_t oc) {
+    return oc > kOrdZero ? CLS_PORE
+           : (oc != 0u && oc < othr) ? CLS_MARKER
+           : (oc == 0u || oc < kOrdZero) ? CLS_FLOOD
+                                         : CLS_ZERO;
+  };
+  if (nx >= 3 && ny >= 3 && nz >= 3) {  // block-uniform
+    // Every axis has three distinct wrapped positions around each voxel, so the lexicographic
+    // maximum of (value key, wrapped index) is: the largest value key (a plain 32-bit maximum,
+    // separable), then among the candidates holding it the one of largest wrapped index, i.e.
+    // the highest-ranked plane, then row, then column. The rank order of (c-1, c, c+1) is
+    // natural unless c-1 wraps to n-1 (c == 0: c-1 ranks first) or c+1 wraps to 0
+    // (c == n-1: c+1 ranks last). Plane maxima of the last three planes sit in a register
+    // window; the winner's row and column are found again from shared memory.
+    const int rx = gx == 0 ? 1 : (gx == nx - 1 ? 2 : 0);
+    const int ry = gy == 0 ? 1 : (gy == ny - 1 ? 2 : 0);
+    auto rowmax = [&](int hz, int hy) {
+      const uint32_t* row = &so[hz][hy][lane];
+      return max(max(row[0], row[1]), row[2]);
+    };
+    uint32_t w0 = 0, w1 = 0, w2 = 0;
+#pragma unroll 1
+    for (int hz = 0; hz < HZ; ++hz) {
+      const uint32_t pm = max(max(rowmax(hz, ty), rowmax(hz, ty + 1)), rowmax(hz, ty + 2));
+      w0 = w1;
+      w1 = w2;
+      w2 = pm;
+      if (hz < 2) continue;
+      const int tz = hz - 2;  // output plane: its z-neighbours are the window's planes
+      const int gz = Z0 + tz;
+      const bool valid = inxy && gz < nz;
+      const int ci = gz * nxy + gy * nx + gx;
+      const uint32_t oc = so[tz + 1][ty + 1][tx + 1];
+      const int cls = voxel_class(oc);
+      int bk = kSelf;
+      if (valid) {
+        const bool up = oc > kOrdZero || oc == 0u;  // !(sdf <= 0): where walks start, peaks sit
+        if (ALL_ASCENT || up) {
+          if (oc != 0u) {  // a NaN voxel stays on itself
+            const uint32_t v = max(max(w0, w1), w2);
+            const int rz = gz == 0 ? 1 : (gz == nz - 1 ? 2 : 0);
+            const int dz = pick_ranked((w0 == v) | ((w1 == v) << 1) | ((w2 == v) << 2), rz);
+            const int pz = tz + dz;
+            const int dy = pick_ranked((rowmax(pz, ty) == v) | ((rowmax(pz, ty + 1) == v) << 1) |
+                                           ((rowmax(pz, ty + 2) == v) << 2),
+                                       ry);
+            const uint32_t* row = &so[pz][ty + dy][lane];
+            const int dx =
+                pick_ranked((row[0] == v) | ((row[1] == v) << 1) | ((row[2] == v) << 2), rx);
+            bk = 9 * dz + 3 * dy + dx;
+          }
+          const int nb = bk == kSelf ? ci
+                                     : wz[tz + bk / 9] * nxy + wy[ty + (bk / 3) % 3] * nx +
+                                           wx[lane + bk % 3];
+          nxt[ci] = off + nb;
+          if (up && bk == kSelf) atomicOr(&peakbits[ci >> 5], 1u << (ci & 31));
+        }
+      }
+      finish_voxel(tz, valid, ci, cls, bk);
+    }
+    return;
+  }
+  // Volumes with an axis of fewer than three voxels: wrapped neighbours can coincide with each
+  // other or with the voxel itself, so candidates are compared as (value key, wrapped index)
+  // pairs throughout.
   // x positions of the three candidates of this lane and the y offsets of this warp's rows
   const uint32_t px0 = wx[lane], px1 = wx[lane + 1], px2 = wx[lane + 2];
   const uint32_t py[3] = {(uint32_t)(wy[ty] * nx), (uint32_t)(wy[ty + 1] * nx),
@@ -157,19 +266,10 @@ __global__ void __launch_bounds__(TX* TY, 8)  // 8 resident tiles per SM (32 reg
     const bool valid = inxy && gz < nz;
     const int ci = gz * nxy + gy * nx + gx;
     const uint32_t oc = so[tz + 1][ty + 1][tx + 1];
-    const int cls = oc > kOrdZero ? CLS_PORE
-                    : (oc != 0u && oc < othr) ? CLS_MARKER
-                    : (oc == 0u || oc < kOrdZero) ? CLS_FLOOD
-                                                  : CLS_ZERO;
-    // flood seed: a marker among the 26 neighbours (the voxel itself is no marker)
-    unsigned nb = 0;
-    if (__any_sync(0xffffffffu, valid && cls == CLS_FLOOD)) {
-#pragma unroll
-      for (int k = 0; k < 9; ++k) nb |= rowd[tz + k / 3][ty + k % 3];
-    }
+    const int cls = voxel_class(oc);
+    int bk = kSelf;
     if (valid) {
       const bool up = oc > kOrdZero || oc == 0u;  // !(sdf <= 0): where walks start, peaks sit
-      int bk = kSelf;
       if (ALL_ASCENT || up) {
         uint32_t bo = wo[0], bp = wp[0];
         int bd = wd[0];
@@ -188,20 +288,8 @@ __global__ void __launch_bounds__(TX* TY, 8)  // 8 resident tiles per SM (32 reg
         nxt[ci] = off + (bk == kSelf ? ci : (int)bp);
         if (up && bk == kSelf) atomicOr(&peakbits[ci >> 5], 1u << (ci & 31));
       }
-      const bool seed = cls == CLS_FLOOD && ((nb >> lane) & 1u);
-      code[ci] = make_code(bk, cls, seed);
     }
-    // marker runs of this chunk row
-    const unsigned m = rowm[tz + 1][ty + 1];
-    const bool marker = valid && ((m >> lane) & 1u);
-    const int hl = marker ? 31 - __clz((m & ~(m << 1)) & upto) : 0;
-    const int head = off + gz * nxy + gy * nx + X0 + hl;
-    if (valid) L[ci] = marker ? head : kBig;
-    if (lane == 0 && gy < ny && gz < nz) {
-      const int xe = nx - X0;  // valid x positions of this chunk
-      mbits[bx.word0 + (gz * ny + gy) * ((nx + 31) >> 5) + (X0 >> 5)] =
-          m & (xe >= 32 ? 0xffffffffu : ((1u << xe) - 1u));
-    }
+    finish_voxel(tz, valid, ci, cls, bk);
   }
 }
 
@@ -739,6 +827,8 @@ __device__ __forceinline__ void hash_insert(unsigned long long* table, uint64_t 
 // only differing faces look their labels up. The seg output needs every label: a warp's row of
 // ids is mapped with one lookup per run of lanes holding the same id.
 struct KeyLabels {
+  // faces compare keys, and the set holds key pairs (mapped to label pairs once per unique pair)
+  static constexpr bool kKeyPairs = true;
   const int* key;
   const int* L;
   __device__ int id(int v, bool active) const { return active ? __ldg(&key[v]) : KEY_NONE; }
@@ -757,6 +847,7 @@ struct KeyLabels {
   __device__ KeyLabels at(int off) const { return KeyLabels{key + off, L}; }
 };
 struct SegLabels {
+  static constexpr bool kKeyPairs = false;
   const int* seg;
   __device__ int id(int v, bool active) const { return active ? __ldg(&seg[v]) : 0; }
   __device__ int label(int k) const { return k; }
@@ -808,10 +899,14 @@ __global__ void __launch_bounds__(STX* STY)
         const int k1 = dd == 0 ? kx : (dd == 1 ? ky : kz);
         uint64_t pk = kEmpty;
         if (in && k1 != k0) {
-          const int g0 = gb + s0, g1 = gb + lab.label(k1);
-          pk = pair_key(g0, g1);
-          lmin = min(lmin, min(g0, g1));
-          lmax = max(lmax, max(g0, g1));
+          if (Lab::kKeyPairs) {
+            pk = pair_key(k0, k1);
+          } else {
+            const int g0 = gb + s0, g1 = gb + lab.label(k1);
+            pk = pair_key(g0, g1);
+            lmin = min(lmin, min(g0, g1));
+            lmax = max(lmax, max(g0, g1));
+          }
         }
         const uint64_t pp = __shfl_up_sync(0xffffffffu, pk, 1);
         if (pk != kEmpty && (lane == 0 || pp != pk))
@@ -823,7 +918,7 @@ __global__ void __launch_bounds__(STX* STY)
       cur = lab.labels_warp(kz, in);
     }
   }
-  if (want_pairs) {
+  if (want_pairs && !Lab::kKeyPairs) {
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
       lmin = min(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
@@ -852,6 +947,33 @@ __global__ void k_hash_gather(const unsigned long long* __restrict__ table, long
     if (k == kEmpty) continue;
     const int lo = (int)((uint32_t)(k >> 32) ^ 0x80000000u);
     const int hi = (int)((uint32_t)k ^ 0x80000000u);
+    const uint32_t dlo = (uint32_t)lo - (uint32_t)base, dhi = (uint32_t)hi - (uint32_t)base;
+    keys[pos[i]] = ((uint64_t)dlo << b) | (uint64_t)dhi;
+  }
+}
+
+// Key pairs -> label pairs: a key's label is its id in L (pore key = basin root; solid key =
+// ~label root; KEY_NONE = debris, label 0); in a batch the label is offset by its volume's pair
+// base, the volume being that of the pair's voxel key (a KEY_NONE face always pairs with a key of
+// its own volume). Then re-encoded as (lo - base) << b | (hi - base) like k_hash_gather.
+template <class G>
+__global__ void k_hash_gather_keys(const unsigned long long* __restrict__ table, long long cap,
+                                   const unsigned* __restrict__ pos, G geo,
+                                   const int* __restrict__ L, const int* range, int b,
+                                   uint64_t* __restrict__ keys) {
+  const int base = range[0];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cap;
+       i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long k = table[i];
+    if (k == kEmpty) continue;
+    const int ka = (int)((uint32_t)(k >> 32) ^ 0x80000000u);
+    const int kb = (int)((uint32_t)k ^ 0x80000000u);
+    const int va = ka >= 0 ? ka : (key_is_solid(ka) ? ~ka : -1);
+    const int vb = kb >= 0 ? kb : (key_is_solid(kb) ? ~kb : -1);
+    const int vol = geo.vol_of(va >= 0 ? va : vb);
+    const int gb = geo.gbase(vol);
+    const int la = gb + label_of_key(L, ka), lb = gb + label_of_key(L, kb);
+    const int lo = min(la, lb), hi = max(la, lb);
     const uint32_t dlo = (uint32_t)lo - (uint32_t)base, dhi = (uint32_t)hi - (uint32_t)base;
     keys[pos[i]] = ((uint64_t)dlo << b) | (uint64_t)dhi;
   }
@@ -965,9 +1087,10 @@ __global__ void k_pores_emit_batch(const float* __restrict__ sdf, VolTab geo,
   }
 }
 
+// Pair labels of a batch are gbase + label >= 0: the sort keys count from 0.
 __global__ void k_batch_init(int* range) {
-  range[0] = INT_MAX;
-  range[1] = INT_MIN;
+  range[0] = 0;
+  range[1] = 0;
 }
 
 // Per-volume label counts (rank differences over the volume's words) and pair-label bases: an
@@ -1282,7 +1405,9 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
     PNM_TRY(c.buf(S_HASH, want_pairs ? cap : 1, &table));
     PNM_TRY(c.buf(S_MAXBITS, 2, &range));
     if (want_pairs) PNM_CUDA(cudaMemsetAsync(table, 0xff, cap * sizeof(unsigned long long), s));
-    const int init[2] = {INT_MAX, INT_MIN};
+    // key pairs: the label range is known ([-nS, nP]); label pairs of a given seg: tracked
+    const int init[2] = {from_keys ? -st->n_solid_labels : INT_MAX,
+                         from_keys ? st->n_pore_labels : INT_MIN};
     PNM_CUDA(cudaMemcpyAsync(range, init, sizeof(init), cudaMemcpyHostToDevice, s));
     PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_ERR], 0, sizeof(unsigned), s));
     PNM_CUDA(cudaMemsetAsync(&c.d_cnt[CNT_PAIRS], 0, sizeof(unsigned), s));
@@ -1335,9 +1460,11 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
     PNM_TRY(c.buf(S_PAIRS, 2 * m + 2, &out));
     *d_pairs_out = out;
     if (m == 0) return Status::ok();
-    int hr[2];
-    PNM_CUDA(cudaMemcpyAsync(hr, range, sizeof(hr), cudaMemcpyDeviceToHost, s));
-    PNM_CUDA(cudaStreamSynchronize(s));
+    int hr[2] = {init[0], init[1]};
+    if (!from_keys) {
+      PNM_CUDA(cudaMemcpyAsync(hr, range, sizeof(hr), cudaMemcpyDeviceToHost, s));
+      PNM_CUDA(cudaStreamSynchronize(s));
+    }
     const unsigned long long span = (unsigned long long)((long long)hr[1] - (long long)hr[0]);
     int b = 1;
     while (b < 32 && (1ull << b) <= span) ++b;
@@ -1349,7 +1476,12 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
     PNM_TRY(c.buf(S_KEYS_B, m, &kb));
     PNM_TRY(c.buf(S_RSHIST, 256 * (m / RS_TILE + 1) + 1, &hist));
     exclusive_scan(Occupied{table}, cap, pos, scan0, s, &c.launches);
-    k_hash_gather<<<grid_for(cap, 256, c.sm_count), 256, 0, s>>>(table, cap, pos, range, b, ka); ++c.launches;
+    if (from_keys)
+      k_hash_gather_keys<<<grid_for(cap, 256, c.sm_count), 256, 0, s>>>(table, cap, pos, geo,
+                                                                        st->idtab, range, b, ka);
+    else
+      k_hash_gather<<<grid_for(cap, 256, c.sm_count), 256, 0, s>>>(table, cap, pos, range, b, ka);
+    ++c.launches;
     const bool in_b = radix_sort(ka, nullptr, kb, nullptr, m, 0, 2 * b, hist, scan0, s, &c.launches);
     k_pairs_decode<<<grid_for(m, 256, c.sm_count), 256, 0, s>>>(in_b ? kb : ka, m, range, b, out); ++c.launches;
     PNM_CUDA(cudaGetLastError());
@@ -1454,7 +1586,8 @@ Status enqueue_batch(BatchPlan& p, cudaStream_t s, long long* launches) {
   exclusive_scan(Occupied{p.table}, p.hash_cap, p.hpos, p.scan_tmp, s, launches);
   const unsigned* m_p = p.hpos + p.hash_cap;
   const unsigned hgrid = grid_for(p.hash_cap, 256, sm);
-  k_hash_gather<<<hgrid, 256, 0, s>>>(p.table, p.hash_cap, p.hpos, p.range, p.label_bits, p.ka);
+  k_hash_gather_keys<<<hgrid, 256, 0, s>>>(p.table, p.hash_cap, p.hpos, geo, p.L, p.range,
+                                           p.label_bits, p.ka);
   p.pairs_in_b = radix_sort(p.ka, nullptr, p.kb, nullptr, p.hash_cap, 0, 2 * p.label_bits, p.hist,
                             p.scan_tmp, s, launches, m_p);
   const uint64_t* sorted = p.pairs_in_b ? p.kb : p.ka;
