@@ -168,6 +168,15 @@ int pnm_extract_pore_network_dev(pnm_ctx* ctx, const float* d_sdf, int32_t nx, i
                                  int32_t* d_seg, int32_t* d_pairs, int64_t pair_cap,
                                  int64_t* n_pairs);
 
+/* The peak voxel of every pore, in the order of the pore records (voxel order): the voxel the
+ * record's SDF^2-weighted centroid is refined around, whose SDF value is the record's radius
+ * (pore_extraction.hpp:89-127). The distributed surface assigns each pore to the rank whose
+ * block holds this voxel, as the reference's extract_pore_network_mpi keeps the pores whose peak
+ * its block owns (pore_extraction_mpi.hpp:208-212, :308-368). At most min(cap, 1e6) ids are
+ * written; *n_peaks receives the count (PNM_ERR_CAPACITY when it exceeds cap). */
+int pnm_pore_peaks_dev(pnm_ctx* ctx, const float* d_sdf, int32_t nx, int32_t ny, int32_t nz,
+                       int32_t* d_voxels, int64_t cap, int64_t* n_peaks);
+
 /* segment_volume on a device SDF into a device seg buffer. */
 int pnm_segment_volume_dev(pnm_ctx* ctx, const float* d_sdf, int32_t nx, int32_t ny, int32_t nz,
                            const float spacing_xyz[3], int32_t* d_seg);

@@ -35,7 +35,8 @@ __all__ = ["Pore", "extract_pores", "segment_volume", "extract_topology_gpu",
            "PnmError", "Batch", "extract_pore_network_batch", "batch_plan_bytes", "Server",
            "SDFReader", "read_vti_device", "save_vti", "write_sdf_vti", "write_edge_list",
            "segment_volume_device", "extract_pore_network_device", "extract_network_flow_device",
-           "network_stats", "throat_conductance"]
+           "network_stats", "throat_conductance", "mpi_rank", "mpi_size", "mpi_block",
+           "extract_pore_network_mpi", "extract_network_flow_mpi"]
 
 execution_space = _capi.pnm_execution_space().decode()
 
@@ -45,6 +46,8 @@ from .vti import SDFReader, read_vti_device, save_vti, write_edge_list, write_sd
 from .device import (extract_network_flow_device, extract_pore_network_device,  # noqa: E402
                      segment_volume_device)
 from .post import network_stats, throat_conductance  # noqa: E402
+from .distributed import (extract_network_flow_mpi, extract_pore_network_mpi,  # noqa: E402
+                          mpi_block, mpi_rank, mpi_size)
 
 
 class Pore:

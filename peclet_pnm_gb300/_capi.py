@@ -94,6 +94,8 @@ pnm_extract_pores = _sig("pnm_extract_pores", ctypes.c_int, _vp, _vp, _i32, _i32
                          _P(_P(PnmPore)), _P(_i64))
 pnm_segment_volume = _sig("pnm_segment_volume", ctypes.c_int, _vp, _vp, _i32, _i32, _i32, _vp,
                           _vp)
+pnm_pore_peaks_dev = _sig("pnm_pore_peaks_dev", ctypes.c_int, _vp, _vp, _i32, _i32, _i32, _vp,
+                          _i64, _P(_i64))
 pnm_segment_volume_dev = _sig("pnm_segment_volume_dev", ctypes.c_int, _vp, _vp, _i32, _i32, _i32,
                               _vp, _vp)
 pnm_extract_topology = _sig("pnm_extract_topology", ctypes.c_int, _vp, _vp, _i32, _i32, _i32,
@@ -200,7 +202,7 @@ EXPORTED = ["pnm_ctx_create", "pnm_ctx_destroy", "pnm_last_error", "pnm_ctx_set_
             "pnm_ctx_trim", "pnm_execution_space", "pnm_free", "pnm_extract_pores",
             "pnm_segment_volume", "pnm_extract_topology", "pnm_extract_pore_network",
             "pnm_extract_network_flow", "pnm_flow_result_free", "pnm_extract_pore_network_dev",
-            "pnm_segment_volume_dev", "pnm_ctx_get_stats", "pnm_ctx_set_timing",
+            "pnm_segment_volume_dev", "pnm_pore_peaks_dev", "pnm_ctx_get_stats", "pnm_ctx_set_timing",
             "pnm_ctx_set_wait_limit", "pnm_extract_pores_noalloc",
             "pnm_batch_plan_bytes", "pnm_batch_create", "pnm_batch_destroy",
             "pnm_batch_last_error", "pnm_batch_stream", "pnm_batch_set_sdf", "pnm_batch_sdf_dev",

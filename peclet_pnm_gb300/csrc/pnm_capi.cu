@@ -391,6 +391,31 @@ int pnm_segment_volume(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t ny, i
   return finish(ctx, run());
 }
 
+int pnm_pore_peaks_dev(pnm_ctx* ctx, const float* d_sdf, int32_t nx, int32_t ny, int32_t nz,
+                       int32_t* d_voxels, int64_t cap, int64_t* n_peaks) {
+  if (!ctx) return PNM_ERR_ARG;
+  Ctx& c = ctx->c;
+  auto run = [&]() -> Status {
+    if (!n_peaks) return Status{PNM_ERR_ARG, "null argument"};
+    *n_peaks = 0;
+    const Dims d{nx, ny, nz};
+    const float unit[3] = {1.0f, 1.0f, 1.0f};  // peaks do not depend on the spacing
+    PNM_TRY(pnm::check_dims(d, unit, true));
+    if (d.n() == 0) return Status::ok();
+    if (!d_sdf || (!d_voxels && cap > 0)) return Status{PNM_ERR_ARG, "null argument"};
+    PNM_TRY(enter(c));
+    pnm::SegState st;
+    PNM_TRY(pnm::run_sdf_pass(c, d_sdf, d, unit, &st));
+    int64_t np = 0;
+    PNM_TRY(pnm::run_peak_ids(c, st, d_voxels, std::min<int64_t>(cap, kMaxPores), &np));
+    np = std::min(np, kMaxPores);
+    *n_peaks = np;
+    if (np > cap) return Status{PNM_ERR_CAPACITY, "device output capacity too small"};
+    return Status::ok();
+  };
+  return finish(ctx, run());
+}
+
 int pnm_segment_volume_dev(pnm_ctx* ctx, const float* d_sdf, int32_t nx, int32_t ny, int32_t nz,
                            const float spacing_xyz[3], int32_t* d_seg) {
   if (!ctx) return PNM_ERR_ARG;

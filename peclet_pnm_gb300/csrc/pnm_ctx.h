@@ -214,6 +214,8 @@ Status run_pores(Ctx& c, const SegState& st, const float origin[3], const float 
 void launch_pores_emit(const float* sdf, Dims d, const uint32_t* bits, const unsigned* pref,
                        long long words, const float origin[3], const float spacing[3],
                        pnm_pore* out, long long cap, unsigned grid, cudaStream_t s);
+// Peak voxel ids of the pore records (voxel order, <= cap written; the count in *n_peaks).
+Status run_peak_ids(Ctx& c, const SegState& st, int32_t* d_out, int64_t cap, int64_t* n_peaks);
 // SDF pass only (for extract_pores alone).
 Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st,
                     bool all_ascent = false, HostXfer* xfer = nullptr);

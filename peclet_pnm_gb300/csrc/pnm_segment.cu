@@ -1056,6 +1056,24 @@ void launch_pores_emit(const float* sdf, Dims d, const uint32_t* bits, const uns
                                     spacing[0], spacing[1], spacing[2], out, cap);
 }
 
+// The voxel id of every set bit of the peak bitmap, at its prefix rank (voxel order): the voxel
+// each pore record of k_pores_emit is centred on.
+__global__ void k_peak_ids(const uint32_t* __restrict__ bits, const unsigned* __restrict__ pref,
+                           long long words, int* __restrict__ out, long long cap) {
+  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < words;
+       w += (long long)gridDim.x * blockDim.x) {
+    uint32_t b = bits[w];
+    unsigned r = pref[w];
+    while (b) {
+      const int j = __ffs(b) - 1;
+      b &= b - 1;
+      if ((long long)r < cap) out[r] = (int)(w * 32 + j);
+      ++r;
+    }
+  }
+}
+
+
 // ---- 8. batch bookkeeping -----------------------------------------------------------------------
 // One pore per set bit of the peak bitmap of a whole batch; a word's volume is found from its
 // first voxel (volumes start on word boundaries). Records land at the batch-wide rank, so each
@@ -1522,6 +1540,25 @@ Status run_pores(Ctx& c, const SegState& st, const float origin[3], const float 
   PNM_CUDA(cudaMemcpyAsync(&tot, pref + words, 4, cudaMemcpyDeviceToHost, s));
   PNM_CUDA(cudaStreamSynchronize(s));
   *n_pores = tot;
+  return Status::ok();
+}
+
+Status run_peak_ids(Ctx& c, const SegState& st, int32_t* d_out, int64_t cap, int64_t* n_peaks) {
+  StageScope stage(c, PNM_STAGE_PORES, "pnm::extract_pores(peak voxels)");
+  cudaStream_t s = c.stream;
+  const long long words = (st.d.n() + 31) / 32;
+  unsigned *pref, *scan0;
+  PNM_TRY(c.buf(S_PEAKPREF, words + 1, &pref));
+  PNM_TRY(c.buf(S_SCAN1, words / SCAN_TILE + 2, &scan0));
+  exclusive_scan(PopcountOf{st.peakbits}, words, pref, scan0, s, &c.launches);
+  k_peak_ids<<<grid_for(words, 256, c.sm_count), 256, 0, s>>>(st.peakbits, pref, words, d_out,
+                                                              cap);
+  ++c.launches;
+  PNM_CUDA(cudaGetLastError());
+  unsigned tot = 0;
+  PNM_CUDA(cudaMemcpyAsync(&tot, pref + words, 4, cudaMemcpyDeviceToHost, s));
+  PNM_CUDA(cudaStreamSynchronize(s));
+  *n_peaks = tot;
   return Status::ok();
 }
 
