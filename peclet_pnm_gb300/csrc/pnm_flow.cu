@@ -521,92 +521,119 @@ struct FluxParams {
   int sq, sa, sc;  // fixed-point scales: fluxes/residuals, areas, centroid moments
 };
 
-// throat_flux (:883-942): for every +d face whose flow labels differ, q = o*vel*A on the +d
-// neighbour's -d face; resid[a-1] += q, resid[b-1] -= q; faces of a patch add +-q, o*A and the
-// area-weighted centroid moment (min-imaged against the lower pore's peak voxel) to their throat.
+// pore_residual (:883-942) per cell: resid[a-1] += q over every +d face whose flow labels differ
+// and resid[b-1] -= q on the other side. A cell takes both roles itself: +q over its own +d faces
+// (fields of the +d neighbour, as the reference's face loop reads them) and -q over its -d faces
+// (its own fields), so each cell has one target (its own label) and each warp one segmented
+// sum. q is rounded the same on both sides and to_fixed(-q) == -to_fixed(q), so the integer
+// sums are exactly those of a face-by-face loop.
 __global__ void __launch_bounds__(256)
-    k_flux(Dims d, const int* __restrict__ flowLab, FieldPtrs f, FaceIndex fx,
-           const int* __restrict__ label, const int* __restrict__ slotOf,
-           const int* __restrict__ peak, FluxParams P, unsigned long long* accR,
-           unsigned long long* accQ, unsigned long long* accA, unsigned long long* accCx,
-           unsigned long long* accCy, unsigned long long* accCz) {
+    k_flux_resid(Dims d, const int* __restrict__ flowLab, FieldPtrs f, FluxParams P,
+                 unsigned long long* accR) {
   const long long n = d.n();
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int nx = d.nx, ny = d.ny, nz = d.nz, nxy = nx * ny;
   for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
        base += (long long)gridDim.x * blockDim.x) {
     const long long c = base + threadIdx.x;
-    const bool valid = c < n;
-    int3 q = make_int3(0, 0, 0);
-    int a = 0;
-    if (valid) {
-      q = coords_of(c, nx, ny);
-      a = flowLab[c];
-    }
-#pragma unroll 1
-    for (int dd = 0; dd < 3; ++dd) {
-      int ta = -1, tb = -1, ts = -1;
-      I128 vq{0ull, 0ll}, vnq{0ull, 0ll}, vQ{0ull, 0ll}, vA{0ull, 0ll}, vC[3];
-      vC[0] = vC[1] = vC[2] = I128{0ull, 0ll};
-      if (valid) {
-        const long long nb = ((long long)(dd == 2 ? wrap1(q.z + 1, nz) : q.z) * ny +
-                              (dd == 1 ? wrap1(q.y + 1, ny) : q.y)) * nx +
-                             (dd == 0 ? wrap1(q.x + 1, nx) : q.x);
-        const int b = flowLab[nb];
-        if (a != b) {
-          const double opn = openness(f, dd, nb);
-          const double area = P.area[dd];
-          const double qv = __dmul_rn(__dmul_rn(opn, velocity(f, dd, nb)), area);
-          if (a > 0) {
-            ta = a - 1;
-            vq = to_fixed(qv, P.sq);
-          }
-          if (b > 0) {
-            tb = b - 1;
-            vnq = to_fixed(-qv, P.sq);
-          }
-          const long long fl = 3 * c + dd;
-          if (bitmap_test(fx.ifbits, fl)) {
-            const unsigned k = bitmap_rank(fx.ifbits, fx.ifpref, fl);
-            ts = slotOf[label[k]];
-            const int lo = a < b ? a : b;
-            const double w0 = __dmul_rn(opn, area);
-            vQ = to_fixed(a < b ? qv : -qv, P.sq);
-            vA = to_fixed(w0, P.sa);
-            const int pk = peak[lo - 1];
-            const int3 pc = coords_of(pk, nx, ny);
-            const int ci[3] = {q.x, q.y, q.z};
-            const int pi[3] = {pc.x, pc.y, pc.z};
+    int target = -1;
+    I128 sum{0ull, 0ll};
+    if (c < n) {
+      const int ci = (int)c;
+      const int z = ci / nxy, r = ci - z * nxy, y = r / nx, x = r - y * nx;
+      const int a = flowLab[ci];
+      if (a > 0) {
+        target = a - 1;
+        int up[3], dn[3];
+        up[0] = ci - x + (x + 1 == nx ? 0 : x + 1);
+        dn[0] = ci - x + (x == 0 ? nx - 1 : x - 1);
+        up[1] = ci + ((y + 1 == ny ? 0 : y + 1) - y) * nx;
+        dn[1] = ci + ((y == 0 ? ny - 1 : y - 1) - y) * nx;
+        up[2] = ci + ((z + 1 == nz ? 0 : z + 1) - z) * nxy;
+        dn[2] = ci + ((z == 0 ? nz - 1 : z - 1) - z) * nxy;
+        int bu[3], bd[3];
 #pragma unroll
-            for (int a2 = 0; a2 < 3; ++a2) {
-              const double fpv = __ldg(&P.F[a2][2 * ci[a2] + (dd == a2 ? 1 : 0)]);
-              const double pcv = __ldg(&P.F[a2][2 * pi[a2]]);
-              double dv = __dsub_rn(fpv, pcv);
-              // minimum image: k = round(dv / L). In half-voxel units the exact difference is
-              // t2 = 2 (c - p) + h; away from |t2| ~ N the rounding errors (< 2^-13 voxel when
-              // P.fast[a2]) cannot move dv/L across +-0.5, so k follows from integers
-              const int t2 = 2 * (ci[a2] - pi[a2]) + (dd == a2 ? 1 : 0);
-              const int at = t2 < 0 ? -t2 : t2;
-              if (!P.fast[a2] || (at > P.N[a2] - 2 && at < P.N[a2] + 2)) {
-                dv = __dsub_rn(dv, __dmul_rn(P.L[a2], round(__ddiv_rn(dv, P.L[a2]))));
-              } else if (at >= P.N[a2] + 2) {
-                dv = __dsub_rn(dv, __dmul_rn(P.L[a2], t2 < 0 ? -1.0 : 1.0));
-              }
-              vC[a2] = to_fixed(__dmul_rn(w0, dv), P.sc);
-            }
+        for (int dd = 0; dd < 3; ++dd) {
+          bu[dd] = flowLab[up[dd]];
+          bd[dd] = flowLab[dn[dd]];
+        }
+#pragma unroll
+        for (int dd = 0; dd < 3; ++dd) {
+          if (bu[dd] != a) {
+            const double qv =
+                __dmul_rn(__dmul_rn(openness(f, dd, up[dd]), velocity(f, dd, up[dd])), P.area[dd]);
+            sum = add128(sum, to_fixed(qv, P.sq));
+          }
+          if (bd[dd] != a) {
+            const double qv =
+                __dmul_rn(__dmul_rn(openness(f, dd, ci), velocity(f, dd, ci)), P.area[dd]);
+            sum = add128(sum, to_fixed(-qv, P.sq));
           }
         }
       }
-      {
-        unsigned long long* const r1[1] = {accR};
-        I128 a1[1] = {vq};
-        warp_accumulate<1>(r1, ta, a1);
-        I128 b1[1] = {vnq};
-        warp_accumulate<1>(r1, tb, b1);
-        unsigned long long* const r5[5] = {accQ, accA, accCx, accCy, accCz};
-        I128 v5[5] = {vQ, vA, vC[0], vC[1], vC[2]};
-        warp_accumulate<5>(r5, ts, v5);
+    }
+    unsigned long long* const r1[1] = {accR};
+    I128 v1[1] = {sum};
+    warp_accumulate<1>(r1, target, v1);
+  }
+}
+
+// Throat sums (:883-942) per compacted interface face k (face order): +-q by the pair's order,
+// o*A, and the area-weighted centroid moment min-imaged against the lower pore's peak voxel, into
+// the face's throat slot. Consecutive faces mostly share a throat: one segmented sum per run.
+__global__ void __launch_bounds__(256)
+    k_flux_throats(Dims d, long long M, const int* __restrict__ fid,
+                   const int* __restrict__ flowLab, FieldPtrs f, const int* __restrict__ label,
+                   const int* __restrict__ slotOf, const int* __restrict__ peak, FluxParams P,
+                   unsigned long long* accQ, unsigned long long* accA, unsigned long long* accCx,
+                   unsigned long long* accCy, unsigned long long* accCz) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz, nxy = nx * ny;
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < M;
+       base += (long long)gridDim.x * blockDim.x) {
+    const long long k = base + threadIdx.x;
+    int ts = -1;
+    I128 vQ{0ull, 0ll}, vA{0ull, 0ll}, vC[3];
+    vC[0] = vC[1] = vC[2] = I128{0ull, 0ll};
+    if (k < M) {
+      const int fl = fid[k];
+      const int ci = fl / 3, dd = fl - 3 * ci;
+      const int z = ci / nxy, r = ci - z * nxy, y = r / nx, x = r - y * nx;
+      const int nb = dd == 0 ? ci - x + (x + 1 == nx ? 0 : x + 1)
+                     : dd == 1 ? ci + ((y + 1 == ny ? 0 : y + 1) - y) * nx
+                               : ci + ((z + 1 == nz ? 0 : z + 1) - z) * nxy;
+      const int a = flowLab[ci], b = flowLab[nb];
+      ts = slotOf[label[k]];
+      const double opn = openness(f, dd, nb);
+      const double area = P.area[dd];
+      const double qv = __dmul_rn(__dmul_rn(opn, velocity(f, dd, nb)), area);
+      const int lo = a < b ? a : b;
+      const double w0 = __dmul_rn(opn, area);
+      vQ = to_fixed(a < b ? qv : -qv, P.sq);
+      vA = to_fixed(w0, P.sa);
+      const int pk = peak[lo - 1];
+      const int pz = pk / nxy, pr = pk - pz * nxy, py = pr / nx, px = pr - py * nx;
+      const int cc[3] = {x, y, z};
+      const int pi[3] = {px, py, pz};
+#pragma unroll
+      for (int a2 = 0; a2 < 3; ++a2) {
+        const double fpv = __ldg(&P.F[a2][2 * cc[a2] + (dd == a2 ? 1 : 0)]);
+        const double pcv = __ldg(&P.F[a2][2 * pi[a2]]);
+        double dv = __dsub_rn(fpv, pcv);
+        // minimum image: k = round(dv / L). In half-voxel units the exact difference is
+        // t2 = 2 (c - p) + h; away from |t2| ~ N the rounding errors (< 2^-13 voxel when
+        // P.fast[a2]) cannot move dv/L across +-0.5, so k follows from integers
+        const int t2 = 2 * (cc[a2] - pi[a2]) + (dd == a2 ? 1 : 0);
+        const int at = t2 < 0 ? -t2 : t2;
+        if (!P.fast[a2] || (at > P.N[a2] - 2 && at < P.N[a2] + 2)) {
+          dv = __dsub_rn(dv, __dmul_rn(P.L[a2], round(__ddiv_rn(dv, P.L[a2]))));
+        } else if (at >= P.N[a2] + 2) {
+          dv = __dsub_rn(dv, __dmul_rn(P.L[a2], t2 < 0 ? -1.0 : 1.0));
+        }
+        vC[a2] = to_fixed(__dmul_rn(w0, dv), P.sc);
       }
     }
+    unsigned long long* const r5[5] = {accQ, accA, accCx, accCy, accCz};
+    I128 v5[5] = {vQ, vA, vC[0], vC[1], vC[2]};
+    warp_accumulate<5>(r5, ts, v5);
   }
 }
 
@@ -850,8 +877,12 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
   unsigned long long* accCx = accA + 2 * ntx;
   unsigned long long* accCy = accCx + 2 * ntx;
   unsigned long long* accCz = accCy + 2 * ntx;
-  k_flux<<<gridn(n, c.sm_count), 256, 0, s>>>(d, flowLab, fp, fx, label, slotOf, peak, P, accR,
-                                               accQ, accA, accCx, accCy, accCz); ++c.launches;
+  k_flux_resid<<<gridn(n, c.sm_count), 256, 0, s>>>(d, flowLab, fp, P, accR); ++c.launches;
+  if (M > 0 && nt > 0) {
+    k_flux_throats<<<gridn(M, c.sm_count), 256, 0, s>>>(d, M, fid, flowLab, fp, label, slotOf,
+                                                         peak, P, accQ, accA, accCx, accCy, accCz);
+    ++c.launches;
+  }
   double* dres;
   PNM_TRY(c.buf(S_FLOWOUT, nacc + ntx, &dres));
   double* resid = dres;
