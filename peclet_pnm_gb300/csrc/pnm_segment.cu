@@ -301,6 +301,17 @@ __global__ void __launch_bounds__(TX* TY, 8)  // 8 resident tiles per SM (32 reg
 // the node covering x_start-1 and every node starting in [x_start, x_end+1] (positions wrap).
 // Links go straight into the union-find (link to the smaller root), so the surviving root of a
 // component is its minimum voxel id, the reference's canonical label (:217-219).
+// node (first voxel of the chunk-local run) covering x of row `row` (z * ny + y) of a volume
+// starting at voxel `off` with bitmap words vb, or -1
+__device__ __forceinline__ int ccl_node_at(const uint32_t* __restrict__ vb, int off, int nx,
+                                           int ncx, int row, int x) {
+  const int c2 = x >> 5, b = x & 31;
+  const uint32_t w = __ldg(&vb[row * ncx + c2]);
+  if (!((w >> b) & 1u)) return -1;
+  const uint32_t st = w & ~(w << 1);
+  return off + row * nx + (c2 << 5) + 31 - __clz(st & ((2u << b) - 1u));
+}
+
 template <class G>
 __global__ void __launch_bounds__(256)
     k_ccl_words(G geo, const uint32_t* __restrict__ mbits, long long n_words, int* L,
@@ -318,14 +329,6 @@ __global__ void __launch_bounds__(256)
     const int c = lw % ncx, row = lw / ncx;
     const int y = row % ny, z = row / ny;
     const uint32_t* vb = mbits + word0;
-    // node (first voxel of the chunk-local run) covering x of row (z2, y2), or -1
-    auto node_at = [&](int z2, int y2, int x) -> int {
-      const int c2 = x >> 5, b = x & 31;
-      const uint32_t w = __ldg(&vb[(z2 * ny + y2) * ncx + c2]);
-      if (!((w >> b) & 1u)) return -1;
-      const uint32_t st = w & ~(w << 1);
-      return off + (z2 * ny + y2) * nx + (c2 << 5) + 31 - __clz(st & ((2u << b) - 1u));
-    };
     uint32_t rem = m;
     while (rem) {
       const int p = __ffs(rem) - 1;
@@ -333,39 +336,46 @@ __global__ void __launch_bounds__(256)
       rem &= len == 32 ? 0u : ~(((1u << len) - 1u) << p);
       const int e = p + len - 1;
       const int xs = (c << 5) + p, xe = (c << 5) + e;
-      const int head = off + (z * ny + y) * nx + xs;
-      int root = head;  // this run's set: carried from link to link
-      auto link = [&](int t) {
-        root = uf_link(L, root, t, err);
-        ++links;
-      };
+      int root = off + row * nx + xs;  // this run's set: carried from link to link
       // +x: the node after the run in this row
       if (xe == nx - 1) {
-        const int t = node_at(z, y, 0);
-        if (t >= 0) link(t);
-      } else if (e == 31 && (__ldg(&vb[(z * ny + y) * ncx + c + 1]) & 1u)) {
-        link(off + (z * ny + y) * nx + ((c + 1) << 5));
+        const int t = ccl_node_at(vb, off, nx, ncx, row, 0);
+        if (t >= 0) {
+          root = uf_link(L, root, t, err);
+          ++links;
+        }
+      } else if (e == 31 && (__ldg(&vb[row * ncx + c + 1]) & 1u)) {
+        root = uf_link(L, root, off + row * nx + ((c + 1) << 5), err);
+        ++links;
       }
-#pragma unroll
+#pragma unroll 1
       for (int f = 0; f < 4; ++f) {
         const int dy = (f == 0 || f == 3) ? 1 : (f == 1 ? -1 : 0), dz = f == 0 ? 0 : 1;
-        const int y2 = wrap1(y + dy, ny), z2 = wrap1(z + dz, nz);
-        const int rowb = off + (z2 * ny + y2) * nx;
-        const int t0 = node_at(z2, y2, xs == 0 ? nx - 1 : xs - 1);
-        if (t0 >= 0) link(t0);
-        const uint32_t w2 = __ldg(&vb[(z2 * ny + y2) * ncx + c]);
+        const int row2 = wrap1(z + dz, nz) * ny + wrap1(y + dy, ny);
+        const int rowb = off + row2 * nx;
+        const int t0 = ccl_node_at(vb, off, nx, ncx, row2, xs == 0 ? nx - 1 : xs - 1);
+        if (t0 >= 0) {
+          root = uf_link(L, root, t0, err);
+          ++links;
+        }
+        const uint32_t w2 = __ldg(&vb[row2 * ncx + c]);
         const int hi = e + 1 > 31 ? 31 : e + 1;
         uint32_t sm = (w2 & ~(w2 << 1)) & ((2u << hi) - 1u) & ~((1u << p) - 1u);
         while (sm) {
           const int b = __ffs(sm) - 1;
           sm &= sm - 1;
-          link(rowb + (c << 5) + b);
+          root = uf_link(L, root, rowb + (c << 5) + b, err);
+          ++links;
         }
         if (xe + 1 == nx) {
-          const int t = node_at(z2, y2, 0);
-          if (t >= 0) link(t);
-        } else if (e == 31 && (__ldg(&vb[(z2 * ny + y2) * ncx + c + 1]) & 1u)) {
-          link(rowb + ((c + 1) << 5));
+          const int t = ccl_node_at(vb, off, nx, ncx, row2, 0);
+          if (t >= 0) {
+            root = uf_link(L, root, t, err);
+            ++links;
+          }
+        } else if (e == 31 && (__ldg(&vb[row2 * ncx + c + 1]) & 1u)) {
+          root = uf_link(L, root, rowb + ((c + 1) << 5), err);
+          ++links;
         }
       }
     }
