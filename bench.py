@@ -77,15 +77,19 @@ def measured_hbm_peak():
 
 
 def profile_traffic():
-    """DRAM bytes per pipeline call from the committed ncu summary (profiles/), if present."""
+    """(DRAM bytes per pipeline call, the commit the ncu capture was taken at) from the committed
+    launch-list summary under profiles/; (None, None) without it."""
     p = os.path.join(ROOT, "profiles", "extract_pore_network_512_launches.txt")
+    traffic = commit = None
     try:
         for line in open(p):
             if line.startswith("dram_bytes_per_call:"):
-                return int(float(line.split(":")[1]))
+                traffic = int(float(line.split(":")[1]))
+            elif line.startswith("taken_at_commit:"):
+                commit = line.split(":")[1].strip()
     except OSError:
         pass
-    return None
+    return traffic, commit
 
 
 def workload_config(n_edge):
@@ -827,7 +831,7 @@ def ours(args, rank, world, local_rank):
 
     peak, peak_src = measured_hbm_peak()
     achieved = ALG_BYTES_PER_VOXEL * nvox / (ms * 1e-3) / 1e9
-    traffic = profile_traffic()
+    traffic, traffic_commit = profile_traffic()
     result = {
         "metric": METRIC, "value": value, "unit": "Gvoxel/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
@@ -835,6 +839,9 @@ def ours(args, rank, world, local_rank):
         "data": "synthetic", "config": workload_config(n_edge),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                       "call, profiles/extract_pore_network_512_launches.txt "
+                                       f"(taken at commit {traffic_commit})",
                      "kernel": "extract_pore_network device pipeline (all kernels of one call)",
                      "model_bytes_per_voxel": ALG_BYTES_PER_VOXEL,
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"},
