@@ -128,14 +128,8 @@ __global__ void __launch_bounds__(TX* TY, 8)  // 8 resident tiles per SM (32 reg
   const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
   // Everything of an output voxel but its ascent direction: class, flood seed, code byte,
   // marker run head and the chunk's marker word.
-  auto finish_voxel = [&](int tz, bool valid, int ci, int cls, int bk) {
+  auto finish_voxel = [&](int tz, bool valid, int ci, int cls, int bk, unsigned nb) {
     const int gz = Z0 + tz;
-    // flood seed: a marker among the 26 neighbours (the voxel itself is no marker)
-    unsigned nb = 0;
-    if (__any_sync(0xffffffffu, valid && cls == CLS_FLOOD)) {
-#pragma unroll
-      for (int k = 0; k < 9; ++k) nb |= rowd[tz + k / 3][ty + k % 3];
-    }
     if (valid) {
       const bool seed = cls == CLS_FLOOD && ((nb >> lane) & 1u);
       code[ci] = make_code(bk, cls, seed);
@@ -173,12 +167,16 @@ __global__ void __launch_bounds__(TX* TY, 8)  // 8 resident tiles per SM (32 reg
       return max(max(row[0], row[1]), row[2]);
     };
     uint32_t w0 = 0, w1 = 0, w2 = 0;
+    unsigned d0 = 0, d1 = 0, d2 = 0;  // marker rows at y-1..y+1 of the last three planes
 #pragma unroll 1
     for (int hz = 0; hz < HZ; ++hz) {
       const uint32_t pm = max(max(rowmax(hz, ty), rowmax(hz, ty + 1)), rowmax(hz, ty + 2));
       w0 = w1;
       w1 = w2;
       w2 = pm;
+      d0 = d1;
+      d1 = d2;
+      d2 = rowd[hz][ty] | rowd[hz][ty + 1] | rowd[hz][ty + 2];
       if (hz < 2) continue;
       const int tz = hz - 2;  // output plane: its z-neighbours are the window's planes
       const int gz = Z0 + tz;
@@ -190,6 +188,7 @@ __global__ void __launch_bounds__(TX* TY, 8)  // 8 resident tiles per SM (32 reg
       if (valid) {
         const bool up = oc > kOrdZero || oc == 0u;  // !(sdf <= 0): where walks start, peaks sit
         if (ALL_ASCENT || up) {
+          int nb = ci;
           if (oc != 0u) {  // a NaN voxel stays on itself
             const uint32_t v = max(max(w0, w1), w2);
             const int rz = gz == 0 ? 1 : (gz == nz - 1 ? 2 : 0);
@@ -202,15 +201,13 @@ __global__ void __launch_bounds__(TX* TY, 8)  // 8 resident tiles per SM (32 reg
             const int dx =
                 pick_ranked((row[0] == v) | ((row[1] == v) << 1) | ((row[2] == v) << 2), rx);
             bk = 9 * dz + 3 * dy + dx;
+            if (bk != kSelf) nb = wz[pz] * nxy + wy[ty + dy] * nx + wx[lane + dx];
           }
-          const int nb = bk == kSelf ? ci
-                                     : wz[tz + bk / 9] * nxy + wy[ty + (bk / 3) % 3] * nx +
-                                           wx[lane + bk % 3];
           nxt[ci] = off + nb;
           if (up && bk == kSelf) atomicOr(&peakbits[ci >> 5], 1u << (ci & 31));
         }
       }
-      finish_voxel(tz, valid, ci, cls, bk);
+      finish_voxel(tz, valid, ci, cls, bk, d0 | d1 | d2);
     }
     return;
   }
@@ -289,7 +286,12 @@ __global__ void __launch_bounds__(TX* TY, 8)  // 8 resident tiles per SM (32 reg
         if (up && bk == kSelf) atomicOr(&peakbits[ci >> 5], 1u << (ci & 31));
       }
     }
-    finish_voxel(tz, valid, ci, cls, bk);
+    unsigned nbm = 0;
+    if (__any_sync(0xffffffffu, valid && cls == CLS_FLOOD)) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) nbm |= rowd[tz + k / 3][ty + k % 3];
+    }
+    finish_voxel(tz, valid, ci, cls, bk, nbm);
   }
 }
 
@@ -386,11 +388,10 @@ __global__ void __launch_bounds__(256)
 }
 
 // ---- 3. resolve ----------------------------------------------------------------------------------
-// Gradient root of a voxel: follow the ascent for at most 512 moves (pore_extraction.hpp:277-309
-// and :626-648; MAX_STEPS = 512). The kernel works on 32 x 8 x 16 bricks whose code bytes sit in
-// shared memory: a walk follows the direction bits there while it stays inside the brick (one
-// move per step, no global load), and continues with the global ascent pointers once it leaves
-// the brick (or would wrap), counting every move, so the cap is exact.
+// Gradient root of a voxel: follow the ascent pointers for at most 512 moves
+// (pore_extraction.hpp:277-309 and :626-648; MAX_STEPS = 512). One thread per voxel, no shared
+// memory: a walk's loads mostly hit L1/L2 (neighbouring walks share their upper parts), and the
+// block stays small enough for full occupancy, which hides the chains' load latency.
 constexpr int RTX = 32, RTY = 8, RTZ = 16;
 
 // For every voxel: marker -> key ~root(CCL), the root joins the key list; pore -> key = gradient
@@ -402,64 +403,30 @@ template <class G>
 __global__ void __launch_bounds__(RTX* RTY)
     k_resolve(G geo, const uint8_t* __restrict__ code, const int* __restrict__ nxt, int* L,
               int* __restrict__ key, int* __restrict__ keylist, unsigned* cnt) {
-  __shared__ uint8_t cb[RTZ][RTY][RTX];
-  __shared__ short nl[RTZ * RTY * RTX];  // in-brick ascent successor (local index), -1: leaves
   unsigned* err = &cnt[CNT_ERR];
   const Box bx = geo.tile(blockIdx.x, RTX, RTY, RTZ, true);
   const int off = bx.off, nx = bx.nx, ny = bx.ny, nz = bx.nz;
   const int nxy = nx * ny;
-  const int X0 = bx.X0, Y0 = bx.Y0, Z0 = bx.Z0;
-  const int TXe = min(RTX, nx - X0), TYe = min(RTY, ny - Y0), TZe = min(RTZ, nz - Z0);
   const int lane = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < RTX * RTY * RTZ; i += RTX * RTY) {
-    const int lx = i % RTX, ly = (i / RTX) % RTY, lz = i / (RTX * RTY);
-    const uint8_t cc = (lx < TXe && ly < TYe && lz < TZe)
-                           ? __ldg(&code[off + (Z0 + lz) * nxy + (Y0 + ly) * nx + X0 + lx])
-                           : make_code(kSelf, CLS_ZERO, false);
-    cb[lz][ly][lx] = cc;
-    const int dk = code_dir(cc);
-    const int x2 = lx + dk % 3 - 1, y2 = ly + (dk / 3) % 3 - 1, z2 = lz + dk / 9 - 1;
-    nl[i] = dk == kSelf ? (short)i
-            : (x2 < 0 || x2 >= TXe || y2 < 0 || y2 >= TYe || z2 < 0 || z2 >= TZe)
-                ? (short)-1
-                : (short)((z2 * RTY + y2) * RTX + x2);
-  }
-  __syncthreads();
-  const bool inxy = lane < TXe && ty < TYe;
+  const int gx = bx.X0 + lane, gy = bx.Y0 + ty;
+  const bool inxy = gx < nx && gy < ny;
+  // the next plane's code byte is loaded while this plane's is used
+  uint8_t cnext = (inxy && bx.Z0 < nz) ? __ldg(&code[off + bx.Z0 * nxy + gy * nx + gx]) : 0;
   for (int tz = 0; tz < RTZ; ++tz) {
-    const bool valid = inxy && tz < TZe;
-    const int v = off + (Z0 + tz) * nxy + (Y0 + ty) * nx + X0 + lane;
+    const int gz = bx.Z0 + tz;
+    const bool valid = inxy && gz < nz;
+    const int v = off + gz * nxy + gy * nx + gx;
+    const uint8_t c = cnext;
+    if (tz + 1 < RTZ) cnext = (inxy && gz + 1 < nz) ? __ldg(&code[v + nxy]) : 0;
     int k = KEY_NONE, agg = -1, par = -1;
     bool new_key = false;
     if (valid) {
-      const uint8_t c = cb[tz][ty][lane];
       const int cls = code_cls(c);
       if (cls == CLS_MARKER) {
         par = ld_cached(&L[v]);  // the run head, or an ancestor of it
       } else if (cls == CLS_PORE) {
-        int li = (tz * RTY + ty) * RTX + lane, moves = 0;
-        bool root = false;
-        while (moves < 512) {  // inside the brick: the successor table
-          const int nli = nl[li];
-          if (nli == li) {
-            root = true;
-            break;
-          }
-          if (nli < 0) break;  // the next move leaves the brick (or wraps)
-          li = nli;
-          ++moves;
-        }
-        const int x = li % RTX, y = (li / RTX) % RTY, z = li / (RTX * RTY);
-        int cur = off + (Z0 + z) * nxy + (Y0 + y) * nx + X0 + x;
-        if (!root) {  // left the brick: the global pointers for the remaining moves
-          for (; moves < 512; ++moves) {
-            const int n2 = __ldg(&nxt[cur]);
-            if (n2 == cur) break;
-            cur = n2;
-          }
-        }
-        k = cur;
-        agg = cur;
+        k = chase_root(nxt, v);
+        agg = k;
       }
     }
     {  // one find per run of lanes sharing a parent (lanes hold consecutive voxels)
@@ -502,7 +469,8 @@ __global__ void __launch_bounds__(TX* TY, 8)
     k_flood_seed(G geo, const uint8_t* __restrict__ code, int* __restrict__ key, int* L,
                  int* __restrict__ ulist, unsigned* cnt) {
   constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2, NT = TX * TY;
-  __shared__ int mk[HZ][HY][HX];  // marker neighbours' keys (~root), INT_MIN elsewhere
+  // per halo row: the largest marker key (~root; INT_MIN for non-markers) over x-1..x+1
+  __shared__ int xm[HZ][HY][TX];
   __shared__ int wx[HX], wy[HY], wz[HZ];
   const Box bx = geo.tile(blockIdx.x, TX, TY, TZ, false);
   const int off = bx.off;
@@ -517,12 +485,21 @@ __global__ void __launch_bounds__(TX* TY, 8)
   if (t < HY) wy[t] = ((Y0 - 1 + t) % ny + ny) % ny;
   if (t < HZ) wz[t] = ((Z0 - 1 + t) % nz + nz) % nz;
   __syncthreads();
+  const int hx = lane == 0 ? 0 : HX - 1;
+  // lane l holds x = X0-1+l+1; lanes 0 and 1 also hold the halo ends x = X0-1 and X0+32
+  auto row_xmax = [&](int r, int km, int kh) {
+    int up = __shfl_up_sync(0xffffffffu, km, 1);
+    int dn = __shfl_down_sync(0xffffffffu, km, 1);
+    const int h1 = __shfl_sync(0xffffffffu, kh, 1);
+    if (lane == 0) up = kh;
+    if (lane == 31) dn = h1;
+    xm[r / HY][r % HY][lane] = max(max(up, km), dn);
+  };
   // halo rows, two per warp iteration with all their loads issued before any is used
   for (int r = t >> 5; r < HY * HZ; r += 2 * (NT / 32)) {
     const int r2 = r + NT / 32;  // warp-uniform
     const int rb = wz[r / HY] * nxy + wy[r % HY] * nx;
     const int rb2 = r2 < HY * HZ ? wz[r2 / HY] * nxy + wy[r2 % HY] * nx : rb;
-    const int hx = lane == 0 ? 0 : HX - 1;
     const uint8_t c0 = __ldg(&code[rb + wx[lane + 1]]);
     const int k0 = __ldg(&key[rb + wx[lane + 1]]);
     const uint8_t c2 = __ldg(&code[rb2 + wx[lane + 1]]);
@@ -535,20 +512,27 @@ __global__ void __launch_bounds__(TX* TY, 8)
       c3 = __ldg(&code[rb2 + wx[hx]]);
       k3 = __ldg(&key[rb2 + wx[hx]]);
     }
-    mk[r / HY][r % HY][lane + 1] = code_cls(c0) == CLS_MARKER ? k0 : INT_MIN;
-    if (lane < 2) mk[r / HY][r % HY][hx] = code_cls(c1) == CLS_MARKER ? k1 : INT_MIN;
-    if (r2 < HY * HZ) {
-      mk[r2 / HY][r2 % HY][lane + 1] = code_cls(c2) == CLS_MARKER ? k2 : INT_MIN;
-      if (lane < 2) mk[r2 / HY][r2 % HY][hx] = code_cls(c3) == CLS_MARKER ? k3 : INT_MIN;
-    }
+    row_xmax(r, code_cls(c0) == CLS_MARKER ? k0 : INT_MIN,
+             code_cls(c1) == CLS_MARKER ? k1 : INT_MIN);
+    if (r2 < HY * HZ)
+      row_xmax(r2, code_cls(c2) == CLS_MARKER ? k2 : INT_MIN,
+               code_cls(c3) == CLS_MARKER ? k3 : INT_MIN);
   }
   __syncthreads();
   const int tx = lane, ty = t >> 5;
   const int gx = X0 + tx, gy = Y0 + ty;
   const bool inxy = gx < nx && gy < ny;
+  auto plane_max = [&](int hz) {
+    return max(max(xm[hz][ty][tx], xm[hz][ty + 1][tx]), xm[hz][ty + 2][tx]);
+  };
+  // the 27-voxel maximum is the 26-neighbour one: the voxel itself (flood) holds no marker key
+  int w0, w1 = plane_max(0), w2 = plane_max(1);
   // the next plane's code byte is loaded while this plane's is used
   uint8_t cnext = (inxy && Z0 < nz) ? __ldg(&code[Z0 * nxy + gy * nx + gx]) : 0;
   for (int tz = 0; tz < TZ; ++tz) {
+    w0 = w1;
+    w1 = w2;
+    w2 = plane_max(tz + 2);
     const int gz = Z0 + tz;
     const bool valid = inxy && gz < nz;
     const int ci = gz * nxy + gy * nx + gx;
@@ -558,12 +542,7 @@ __global__ void __launch_bounds__(TX* TY, 8)
     if (valid) {
       if (code_cls(c) == CLS_FLOOD) {
         if (code_seed(c)) {
-          int bestk = INT_MIN;  // largest marker key == smallest label
-#pragma unroll
-          for (int k = 0; k < 27; ++k) {
-            if (k == kSelf) continue;
-            bestk = max(bestk, mk[tz + k / 9][ty + (k / 3) % 3][tx + k % 3]);
-          }
+          const int bestk = max(max(w0, w1), w2);  // largest marker key == smallest label
           key[ci] = bestk;
           const int lab = ~bestk;
           // first appearance: the label's minimum starts at its root id L[lab] == lab

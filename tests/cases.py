@@ -70,7 +70,23 @@ def edge_cases():
     # thin spacing: marker threshold scales with min spacing
     out.append(("packing_fine_spacing", pk.astype(np.float32) * 0.1, [0.0, 0.0, 0.0],
                 [0.1, 0.1, 0.25]))
+    # walks longer than the cap in volumes of three or more voxels per axis (ties across the
+    # short axes), along x and along z
+    out.append(("walk_cap_3d_x", np.tile(_tent(1300), (3, 3, 1)), *UNIT))
+    out.append(("walk_cap_3d_z", np.tile(_tent(1300)[:, None, None], (1, 3, 3)), *UNIT))
+    out.append(("serpentine_walk", _serpentine(), *UNIT))
     return out
+
+
+def _serpentine():
+    """A pore path snaking through rows y = 1, 3, 5 of a 32-voxel-wide block between walls: the
+    ascent from its start makes ~90 moves without leaving a 32 x 8 x 16 block."""
+    s = np.full((3, 8, 40), -2.0, np.float32)
+    cells = [(1, x) for x in range(1, 31)] + [(2, 30)] + [(3, x) for x in range(30, 0, -1)]
+    cells += [(4, 1)] + [(5, x) for x in range(1, 31)]
+    for p, (y, x) in enumerate(cells):
+        s[:, y, x] = np.float32(1.0 + 0.01 * p)
+    return s
 
 
 def standard_cases():
