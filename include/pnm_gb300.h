@@ -69,7 +69,10 @@ void pnm_free(void* p);
 #define PNM_STAGE_RELABEL 4       /* "pnm::relabel_min" .. "pnm::relabel_assign": label ids */
 #define PNM_STAGE_SEG_PAIRS 5     /* "pnm::relabel_seg" + "pnm::boundary_pairs" */
 #define PNM_STAGE_PAIR_SORT 6     /* unique sorted pairs (the reference sorts on the host) */
-#define PNM_STAGE_PORES 7         /* pore records with their centroids */
+#define PNM_STAGE_PORES 7         /* pore records with their centroids; in extract_pore_network
+                                     calls they run on a second stream, overlapping
+                                     merge_markers and gradient_path (their time is their own
+                                     span, not a share of the call's) */
 #define PNM_STAGE_NETWORK_FLOW 8  /* "nf::*": network flow after the segmentation */
 #define PNM_STAGE_COUNT 9
 

@@ -73,6 +73,24 @@ Status Ctx::ensure_copy_events(int n) {
   return Status::ok();
 }
 
+Status Ctx::ensure_side() {
+  if (side_stream) return Status::ok();
+  PNM_CUDA(cudaStreamCreateWithFlags(&side_stream, cudaStreamNonBlocking));
+  PNM_CUDA(cudaEventCreateWithFlags(&side_fork, cudaEventDisableTiming));
+  PNM_CUDA(cudaEventCreateWithFlags(&side_join, cudaEventDisableTiming));
+  PNM_CUDA(cudaEventCreate(&side_t0));
+  PNM_CUDA(cudaEventCreate(&side_t1));
+  PNM_CUDA(cudaMallocHost(&h_side, 16));
+  return Status::ok();
+}
+
+Status Ctx::join_side() {
+  if (!side_pending) return Status::ok();
+  PNM_CUDA(cudaStreamWaitEvent(stream, side_join, 0));
+  side_pending = false;
+  return Status::ok();
+}
+
 Status Ctx::read_counters() {
   PNM_CUDA(cudaMemcpyAsync(h_cnt, d_cnt, CNT_COUNT * sizeof(unsigned), cudaMemcpyDeviceToHost,
                            stream));
@@ -82,6 +100,7 @@ Status Ctx::read_counters() {
 
 void Ctx::call_begin() {
   for (double& t : last.stage_ms) t = 0.0;
+  side_timed = false;
   tstage.clear();
   open_stages.clear();
 }
@@ -130,6 +149,16 @@ void Ctx::stage_end() {
 }
 
 void Ctx::stage_collect() {
+  if (timing && side_timed) {  // the side stream's interval (it overlaps the main stream's)
+    float ms = 0.0f;
+    if (cudaEventSynchronize(side_t1) == cudaSuccess &&
+        cudaEventElapsedTime(&ms, side_t0, side_t1) == cudaSuccess && side_stage >= 0 &&
+        side_stage < PNM_STAGE_COUNT)
+      last.stage_ms[side_stage] += ms;
+    else
+      cudaGetLastError();
+    side_timed = false;
+  }
   if (!timing || tstage.empty()) return;
   if (cudaEventSynchronize(tev[2 * tstage.size() - 1]) != cudaSuccess) {
     cudaGetLastError();
@@ -224,8 +253,12 @@ Status do_network(Ctx& c, const float* d_sdf, Dims d, const float* org, const fl
                   bool want_pairs, int32_t** d_pairs, int64_t* n_pairs,
                   pnm::HostXfer* xfer = nullptr) {
   pnm::SegState st;
-  PNM_TRY(pnm::run_segmentation(c, d_sdf, d, spc, &st, false, xfer));
-  if (d_pores) PNM_TRY(pnm::run_pores(c, st, org, spc, d_pores, pore_cap, n_pores));
+  // the pore records need the SDF pass alone: they run on the side stream meanwhile
+  const std::function<Status()> pores = [&]() {
+    return pnm::run_pores_side(c, st, org, spc, d_pores, pore_cap);
+  };
+  PNM_TRY(pnm::run_segmentation(c, d_sdf, d, spc, &st, false, xfer, d_pores ? &pores : nullptr));
+  if (d_pores) PNM_TRY(pnm::side_pores_count(c, n_pores));
   PNM_TRY(pnm::run_seg_and_topology(c, st, d_seg, want_pairs, d_pairs, n_pairs, xfer));
   record(c, st, d_pores ? *n_pores : 0, want_pairs ? *n_pairs : 0);
   return Status::ok();
@@ -284,6 +317,13 @@ void pnm_ctx_destroy(pnm_ctx* ctx) {
   }
   for (cudaEvent_t e : c.events) cudaEventDestroy(e);
   for (cudaEvent_t e : c.tev) cudaEventDestroy(e);
+  if (c.side_stream) {
+    cudaStreamSynchronize(c.side_stream);
+    cudaStreamDestroy(c.side_stream);
+    for (cudaEvent_t e : {c.side_fork, c.side_join, c.side_t0, c.side_t1})
+      if (e) cudaEventDestroy(e);
+    if (c.h_side) cudaFreeHost(c.h_side);
+  }
   if (c.own_stream) cudaStreamDestroy(c.own_stream);
   delete ctx;
 }

@@ -7,6 +7,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -56,6 +57,7 @@ enum Counter : int {
   CNT_SWEEPS,        // flood sweeps run by the persistent flood loop
   CNT_BAR0,          // grid barrier of the persistent flood loop: arrivals
   CNT_BAR1,          //   and generation
+  CNT_GATHER,        // hash slots gathered so far (append order)
   CNT_COUNT = 32
 };
 
@@ -68,7 +70,7 @@ enum Slot : int {
   S_U, S_V, S_W, S_P, S_OX, S_OY, S_OZ, S_FLOWLAB, S_FBITS, S_FCORE, S_FPREF, S_FID, S_FPAIR,
   S_FPAR, S_FFILM, S_FMINCORE, S_FLABEL, S_ROOTFLAG, S_SLOTOF, S_PEAK, S_NPORES_OUT,
   S_PPRES, S_REC, S_ACC, S_TDP, S_THROATS, S_MAXBITS, S_FLOWOUT, S_ULIST, S_EDGES, S_NXT, S_STEPS,
-  S_COORD,
+  S_COORD, S_SCAN2, S_HASHKEYS,
   // post-processing
   S_POST, S_POSTCOORD,
   S_COUNT
@@ -115,6 +117,17 @@ struct Ctx {
   void stage_begin(int id, const char* name);  // NVTX push (+ start event)
   void stage_end();                            // (end event +) NVTX pop
   void stage_collect();                        // waits for the events, fills last.stage_ms
+  // Side stream: work that depends on the SDF pass alone (the pore records) runs there while the
+  // main stream runs the marker CCL and the resolve; the main stream joins it before the flood
+  // (whose cooperative launch wants the whole GPU). Its stage interval is timed on its own.
+  cudaStream_t side_stream = nullptr;
+  cudaEvent_t side_fork = nullptr, side_join = nullptr, side_t0 = nullptr, side_t1 = nullptr;
+  bool side_pending = false;  // work enqueued there that the main stream has not joined yet
+  bool side_timed = false;    // side_t0/side_t1 hold this call's side interval
+  int side_stage = 0;
+  unsigned* h_side = nullptr;  // pinned: a count the side stream copied back
+  Status ensure_side();
+  Status join_side();
   std::string last_error;
   Status fail(Status s) {
     last_error = s.msg;
@@ -199,8 +212,11 @@ struct SegState {
 
 // Fused SDF pass + CCL + flood + gradient roots + first-appearance renumbering. all_ascent:
 // also compute the ascent pointer of non-pore voxels (network flow's basins need every cell).
+// after_sdf (optional) runs once the SDF pass is enqueued: it may fork work onto the side
+// stream, which is joined before the flood.
 Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st,
-                        bool all_ascent = false, HostXfer* xfer = nullptr);
+                        bool all_ascent = false, HostXfer* xfer = nullptr,
+                        const std::function<Status()>* after_sdf = nullptr);
 // Writes seg (if d_seg != null) and the unique sorted label pairs (if want_pairs) from the state.
 Status run_seg_and_topology(Ctx& c, const SegState& st, int32_t* d_seg, bool want_pairs,
                             int32_t** d_pairs_out, int64_t* n_pairs, HostXfer* xfer = nullptr);
@@ -210,6 +226,11 @@ Status run_topology_of_seg(Ctx& c, const int32_t* d_seg, Dims d, int32_t** d_pai
 // Compacts the peak bitmap into pores (voxel order, centroid-refined) in d_out (cap entries).
 Status run_pores(Ctx& c, const SegState& st, const float origin[3], const float spacing[3],
                  pnm_pore* d_out, int64_t cap, int64_t* n_pores);
+// run_pores on the side stream, forked from the main stream after the SDF pass; the count
+// is read with side_pores_count once the side stream is joined.
+Status run_pores_side(Ctx& c, const SegState& st, const float origin[3], const float spacing[3],
+                      pnm_pore* d_out, int64_t cap);
+Status side_pores_count(Ctx& c, int64_t* n_pores);
 // Pore records from a peak bitmap and its exclusive word prefix counts (voxel order, <= cap).
 void launch_pores_emit(const float* sdf, Dims d, const uint32_t* bits, const unsigned* pref,
                        long long words, const float origin[3], const float spacing[3],

@@ -329,7 +329,7 @@ struct ValueOf {
 
 // ---- stable LSD radix sort of (uint64 key, uint32 value), 8 bits per pass ------------------------
 constexpr int RS_THREADS = 256;
-constexpr int RS_ROUNDS = 16;
+constexpr int RS_ROUNDS = 4;
 constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
 
 // m_dev (optional): the live key count on the device, at most m; tiles past it stay empty, so a

@@ -7,6 +7,7 @@
 // round-to-nearest intrinsic in the reference's order (and the library is built with
 // -fmad=false).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <climits>
@@ -772,13 +773,11 @@ __device__ __forceinline__ uint64_t pair_key(int a, int b) {
   return ((uint64_t)((uint32_t)lo ^ 0x80000000u) << 32) | (uint64_t)((uint32_t)hi ^ 0x80000000u);
 }
 constexpr uint64_t kEmpty = ~0ull;  // no valid pair key is all ones (lo < hi)
-__device__ __forceinline__ uint64_t mix64(uint64_t x) {
-  x ^= x >> 33;
-  x *= 0xff51afd7ed558ccdull;
-  x ^= x >> 33;
-  x *= 0xc4ceb9fe1a85ec53ull;
-  x ^= x >> 33;
-  return x;
+// Slot hash of a pair key: a 32-bit multiplicative mix of its two halves (the set is kept
+// sparse, so a cheap mix is enough; probing is linear).
+__device__ __forceinline__ uint32_t pair_hash(uint64_t k) {
+  uint32_t h = (uint32_t)(k >> 32) * 0x9e3779b1u ^ (uint32_t)k * 0x85ebca77u;
+  return h ^ (h >> 15);
 }
 constexpr int kMaxProbe = 4096;
 // A slot changes once, from kEmpty to its final key, so a read through L1 that returns an older
@@ -789,16 +788,19 @@ __device__ __forceinline__ unsigned long long ld_slot(const unsigned long long* 
   asm volatile("ld.global.ca.u64 %0, [%1];" : "=l"(v) : "l"(p));
   return v;
 }
+// Inserts k; a new key is counted and, with `dense`, appended there at its count.
 __device__ __forceinline__ void hash_insert(unsigned long long* table, uint64_t mask, uint64_t k,
-                                            unsigned* err, unsigned* count) {
-  uint64_t h = mix64(k) & mask;
+                                            unsigned* err, unsigned* count,
+                                            unsigned long long* dense) {
+  uint64_t h = pair_hash(k) & mask;
   for (int p = 0; p < kMaxProbe; ++p) {
     const unsigned long long cur = ld_slot(&table[h]);
     if (cur == k) return;
     if (cur == kEmpty) {
       const unsigned long long old = atomicCAS(&table[h], kEmpty, (unsigned long long)k);
       if (old == kEmpty) {
-        atomicAdd(count, 1u);
+        const unsigned at = atomicAdd(count, 1u);
+        if (dense) dense[at] = k;
         return;
       }
       if (old == k) return;
@@ -854,7 +856,8 @@ constexpr int STX = 32, STY = 8, STZ = 16;
 template <class G, class Lab>
 __global__ void __launch_bounds__(STX* STY)
     k_seg_topo(G geo, Lab lab_all, int* __restrict__ seg, int want_pairs,
-               unsigned long long* table, uint64_t mask, unsigned* cnt, int* range) {
+               unsigned long long* table, uint64_t mask, unsigned* cnt, int* range,
+               unsigned long long* dense) {
   const Box bx = geo.tile(blockIdx.x, STX, STY, STZ, true);
   const Lab lab = lab_all.at(bx.off);
   if (seg) seg += bx.off;
@@ -899,7 +902,7 @@ __global__ void __launch_bounds__(STX* STY)
         }
         const uint64_t pp = __shfl_up_sync(0xffffffffu, pk, 1);
         if (pk != kEmpty && (lane == 0 || pp != pk))
-          hash_insert(table, mask, pk, &cnt[CNT_ERR], &cnt[CNT_PAIRS]);
+          hash_insert(table, mask, pk, &cnt[CNT_ERR], &cnt[CNT_PAIRS], dense);
       }
     }
     if (z + 1 < z1) {  // warp-uniform
@@ -925,10 +928,16 @@ struct Occupied {
   __device__ unsigned operator()(long long i) const { return t[i] != kEmpty ? 1u : 0u; }
 };
 
-// Gathers the occupied hash slots into dense keys re-encoded as (lo - base) << b | (hi - base).
+// Gathers the occupied hash slots into dense keys re-encoded as (lo - base) << b | (hi - base):
+// at their rank among the occupied slots (pos); or, with `fill` (a zeroed counter), appended in
+// any order (the keys are sorted next); or, with neither, in place (a dense key list).
+__device__ __forceinline__ long long gather_slot(long long i, const unsigned* pos,
+                                                 unsigned* fill) {
+  return fill ? (long long)warp_append(fill, true) : (pos ? (long long)pos[i] : i);
+}
 __global__ void k_hash_gather(const unsigned long long* __restrict__ table, long long cap,
-                              const unsigned* __restrict__ pos, const int* range, int b,
-                              uint64_t* __restrict__ keys) {
+                              const unsigned* __restrict__ pos, unsigned* fill, const int* range,
+                              int b, uint64_t* __restrict__ keys) {
   const int base = range[0];
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cap;
        i += (long long)gridDim.x * blockDim.x) {
@@ -937,7 +946,7 @@ __global__ void k_hash_gather(const unsigned long long* __restrict__ table, long
     const int lo = (int)((uint32_t)(k >> 32) ^ 0x80000000u);
     const int hi = (int)((uint32_t)k ^ 0x80000000u);
     const uint32_t dlo = (uint32_t)lo - (uint32_t)base, dhi = (uint32_t)hi - (uint32_t)base;
-    keys[pos[i]] = ((uint64_t)dlo << b) | (uint64_t)dhi;
+    keys[gather_slot(i, pos, fill)] = ((uint64_t)dlo << b) | (uint64_t)dhi;
   }
 }
 
@@ -947,7 +956,7 @@ __global__ void k_hash_gather(const unsigned long long* __restrict__ table, long
 // its own volume). Then re-encoded as (lo - base) << b | (hi - base) like k_hash_gather.
 template <class G>
 __global__ void k_hash_gather_keys(const unsigned long long* __restrict__ table, long long cap,
-                                   const unsigned* __restrict__ pos, G geo,
+                                   const unsigned* __restrict__ pos, unsigned* fill, G geo,
                                    const int* __restrict__ L, const int* range, int b,
                                    uint64_t* __restrict__ keys) {
   const int base = range[0];
@@ -964,7 +973,7 @@ __global__ void k_hash_gather_keys(const unsigned long long* __restrict__ table,
     const int la = gb + label_of_key(L, ka), lb = gb + label_of_key(L, kb);
     const int lo = min(la, lb), hi = max(la, lb);
     const uint32_t dlo = (uint32_t)lo - (uint32_t)base, dhi = (uint32_t)hi - (uint32_t)base;
-    keys[pos[i]] = ((uint64_t)dlo << b) | (uint64_t)dhi;
+    keys[gather_slot(i, pos, fill)] = ((uint64_t)dlo << b) | (uint64_t)dhi;
   }
 }
 
@@ -1288,12 +1297,13 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
 }
 
 Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st,
-                        bool all_ascent, HostXfer* xfer) {
+                        bool all_ascent, HostXfer* xfer, const std::function<Status()>* after_sdf) {
   const long long n = d.n();
   const long long words = (n + 31) / 32;
   cudaStream_t s = c.stream;
   PNM_CUDA(cudaMemsetAsync(c.d_cnt, 0, CNT_COUNT * sizeof(unsigned), s));
   PNM_TRY(run_sdf_pass(c, d_sdf, d, spacing, st, all_ascent, xfer));
+  if (after_sdf) PNM_TRY((*after_sdf)());
   const OneVol geo{d, marker_threshold(spacing)};
   int* L = st->idtab;
   int *key, *keylist, *f0, *f1, *tmp, *ulist;
@@ -1318,6 +1328,7 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
                                                                         L, key, keylist, c.d_cnt);
     ++c.launches;
   }
+  PNM_TRY(c.join_side());  // the cooperative flood loop below wants every SM to itself
   StageScope flood_stage(c, PNM_STAGE_FLOOD, "pnm::flood");
   k_flood_seed<OneVol, TZ_PLAIN><<<tiles, TX * TY, 0, s>>>(geo, st->code, key, L, ulist, c.d_cnt);
   const unsigned fgrid = grid_for(n, 256, c.sm_count, 4);
@@ -1408,8 +1419,10 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
   for (int attempt = 0; attempt < 8; ++attempt) {
     StageScope stage(c, PNM_STAGE_SEG_PAIRS, "pnm::relabel_seg+boundary_pairs");
     unsigned long long* table = nullptr;
+    unsigned long long* dense = nullptr;  // the set's keys in insertion order
     int* range = nullptr;
     PNM_TRY(c.buf(S_HASH, want_pairs ? cap : 1, &table));
+    if (want_pairs) PNM_TRY(c.buf(S_HASHKEYS, cap, &dense));
     PNM_TRY(c.buf(S_MAXBITS, 2, &range));
     if (want_pairs) PNM_CUDA(cudaMemsetAsync(table, 0xff, cap * sizeof(unsigned long long), s));
     // key pairs: the label range is known ([-nS, nP]); label pairs of a given seg: tracked
@@ -1434,7 +1447,7 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
         geo.base = (int)(z0 / STZ * bpp);
         k_seg_topo<<<(unsigned)(((z1 - z0 + STZ - 1) / STZ) * bpp), STX * STY, 0, s>>>(
             geo, KeyLabels{st->key, st->idtab}, seg_out, want_pairs ? 1 : 0, table,
-            (uint64_t)(cap - 1), c.d_cnt, range);
+            (uint64_t)(cap - 1), c.d_cnt, range, dense);
         ++c.launches;
         PNM_CUDA(cudaEventRecord(c.events[k + i], s));
         PNM_CUDA(cudaStreamWaitEvent(c.copy_stream, c.events[k + i], 0));
@@ -1446,11 +1459,11 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
     } else if (from_keys) {
       k_seg_topo<<<g, STX * STY, 0, s>>>(geo, KeyLabels{st->key, st->idtab}, seg_out,
                                          want_pairs ? 1 : 0, table, (uint64_t)(cap - 1), c.d_cnt,
-                                         range);
+                                         range, dense);
       ++c.launches;
     } else {
       k_seg_topo<<<g, STX * STY, 0, s>>>(geo, SegLabels{d_seg_in}, seg_out, want_pairs ? 1 : 0,
-                                         table, (uint64_t)(cap - 1), c.d_cnt, range);
+                                         table, (uint64_t)(cap - 1), c.d_cnt, range, dense);
       ++c.launches;
     }
     PNM_CUDA(cudaGetLastError());
@@ -1475,19 +1488,19 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
     const unsigned long long span = (unsigned long long)((long long)hr[1] - (long long)hr[0]);
     int b = 1;
     while (b < 32 && (1ull << b) <= span) ++b;
-    unsigned *pos, *scan0, *hist;
+    unsigned *scan0, *hist;
     uint64_t *ka, *kb;
-    PNM_TRY(c.buf(S_SCAN1, cap + 1, &pos));
-    PNM_TRY(c.buf(S_SCAN0, cap / SCAN_TILE + 2 + (256 * (m / RS_TILE + 1)) / SCAN_TILE + 2, &scan0));
+    PNM_TRY(c.buf(S_SCAN0, (256 * (m / RS_TILE + 1)) / SCAN_TILE + 2, &scan0));
     PNM_TRY(c.buf(S_KEYS_A, m, &ka));
     PNM_TRY(c.buf(S_KEYS_B, m, &kb));
     PNM_TRY(c.buf(S_RSHIST, 256 * (m / RS_TILE + 1) + 1, &hist));
-    exclusive_scan(Occupied{table}, cap, pos, scan0, s, &c.launches);
+    // the m keys the inserts appended (no sweep of the set)
     if (from_keys)
-      k_hash_gather_keys<<<grid_for(cap, 256, c.sm_count), 256, 0, s>>>(table, cap, pos, geo,
-                                                                        st->idtab, range, b, ka);
+      k_hash_gather_keys<<<grid_for(m, 256, c.sm_count), 256, 0, s>>>(
+          dense, m, nullptr, nullptr, geo, st->idtab, range, b, ka);
     else
-      k_hash_gather<<<grid_for(cap, 256, c.sm_count), 256, 0, s>>>(table, cap, pos, range, b, ka);
+      k_hash_gather<<<grid_for(m, 256, c.sm_count), 256, 0, s>>>(dense, m, nullptr, nullptr,
+                                                                 range, b, ka);
     ++c.launches;
     const bool in_b = radix_sort(ka, nullptr, kb, nullptr, m, 0, 2 * b, hist, scan0, s, &c.launches);
     k_pairs_decode<<<grid_for(m, 256, c.sm_count), 256, 0, s>>>(in_b ? kb : ka, m, range, b, out); ++c.launches;
@@ -1501,7 +1514,8 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
 Status run_seg_and_topology(Ctx& c, const SegState& st, int32_t* d_seg, bool want_pairs,
                             int32_t** d_pairs_out, int64_t* n_pairs, HostXfer* xfer) {
   const long long labels = (long long)st.n_pore_labels + st.n_solid_labels + 2;
-  const long long hint = std::min<long long>(std::max<long long>(64 * labels, 4096), 3 * st.d.n() + 64);
+  const long long hint =
+      std::min<long long>(std::max<long long>(64 * labels, 4096), 3 * st.d.n() + 64);
   return emit_pairs(c, st.d, true, &st, nullptr, d_seg, want_pairs, hint, d_pairs_out, n_pairs,
                     xfer);
 }
@@ -1529,6 +1543,45 @@ Status run_pores(Ctx& c, const SegState& st, const float origin[3], const float 
   PNM_CUDA(cudaMemcpyAsync(&tot, pref + words, 4, cudaMemcpyDeviceToHost, s));
   PNM_CUDA(cudaStreamSynchronize(s));
   *n_pores = tot;
+  return Status::ok();
+}
+
+Status run_pores_side(Ctx& c, const SegState& st, const float origin[3], const float spacing[3],
+                      pnm_pore* d_out, int64_t cap) {
+  PNM_TRY(c.ensure_side());
+  cudaStream_t s = c.side_stream;
+  struct Range {  // the stage's NVTX range on the host thread
+    Range() { nvtxRangePushA("pnm::extract_pores(records)"); }
+    ~Range() { nvtxRangePop(); }
+  } range;
+  const long long words = (st.d.n() + 31) / 32;
+  unsigned *pref, *scan0;
+  PNM_TRY(c.buf(S_PEAKPREF, words + 1, &pref));
+  PNM_TRY(c.buf(S_SCAN2, words / SCAN_TILE + 2, &scan0));
+  PNM_CUDA(cudaEventRecord(c.side_fork, c.stream));
+  PNM_CUDA(cudaStreamWaitEvent(s, c.side_fork, 0));
+  if (c.timing) PNM_CUDA(cudaEventRecord(c.side_t0, s));
+  exclusive_scan(PopcountOf{st.peakbits}, words, pref, scan0, s, &c.launches);
+  k_pores_emit<<<grid_for(words, 256, c.sm_count), 256, 0, s>>>(
+      st.sdf, st.d, st.peakbits, pref, words, origin[0], origin[1], origin[2], spacing[0],
+      spacing[1], spacing[2], d_out, cap);
+  ++c.launches;
+  PNM_CUDA(cudaGetLastError());
+  PNM_CUDA(cudaMemcpyAsync(c.h_side, pref + words, 4, cudaMemcpyDeviceToHost, s));
+  if (c.timing) {
+    PNM_CUDA(cudaEventRecord(c.side_t1, s));
+    c.side_timed = true;
+    c.side_stage = PNM_STAGE_PORES;
+  }
+  PNM_CUDA(cudaEventRecord(c.side_join, s));
+  c.side_pending = true;
+  return Status::ok();
+}
+
+Status side_pores_count(Ctx& c, int64_t* n_pores) {
+  PNM_TRY(c.join_side());
+  PNM_CUDA(cudaEventSynchronize(c.side_join));
+  *n_pores = *c.h_side;
   return Status::ok();
 }
 
@@ -1605,15 +1658,15 @@ Status enqueue_batch(BatchPlan& p, cudaStream_t s, long long* launches) {
   k_batch_labels<<<1, SCAN_THREADS, 0, s>>>(p.vols, p.res, p.nvol, p.prefP, p.prefS);
   k_seg_topo<<<(unsigned)p.bricks, STX * STY, 0, s>>>(geo, KeyLabels{p.key, p.L}, p.seg, 1,
                                                        p.table, (uint64_t)(p.hash_cap - 1), p.cnt,
-                                                       p.range);
+                                                       p.range, nullptr);
   *launches += 5;
   PNM_CUDA(cudaGetLastError());
   // unique pairs: compact the set, sort, decode per volume (counts stay on the device)
   exclusive_scan(Occupied{p.table}, p.hash_cap, p.hpos, p.scan_tmp, s, launches);
   const unsigned* m_p = p.hpos + p.hash_cap;
   const unsigned hgrid = grid_for(p.hash_cap, 256, sm);
-  k_hash_gather_keys<<<hgrid, 256, 0, s>>>(p.table, p.hash_cap, p.hpos, geo, p.L, p.range,
-                                           p.label_bits, p.ka);
+  k_hash_gather_keys<<<hgrid, 256, 0, s>>>(p.table, p.hash_cap, p.hpos, nullptr, geo, p.L,
+                                           p.range, p.label_bits, p.ka);
   p.pairs_in_b = radix_sort(p.ka, nullptr, p.kb, nullptr, p.hash_cap, 0, 2 * p.label_bits, p.hist,
                             p.scan_tmp, s, launches, m_p);
   const uint64_t* sorted = p.pairs_in_b ? p.kb : p.ka;
