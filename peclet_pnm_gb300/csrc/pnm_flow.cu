@@ -374,9 +374,35 @@ struct FaceIndex {
   const unsigned long long* fpair;
 };
 
-// Visits every interface face of the same pair adjacent to face (c, dd) under the reference's
-// doubled-offset rule |2*dc + e_d2 - e_d|^2 <= 8 over the 27 wrapped neighbour cells
-// (:711-723, :776-791), calling fn(k2, is_core).
+// The reference's adjacency of faces (:711-723, :776-791): face (c, dd) and face (c + dc, d2)
+// are adjacent when |2*dc + e_d2 - e_dd|^2 <= 8. For each dd, the 42 admitted (dc, d2) as bytes
+// (dz+1) << 6 | (dy+1) << 4 | (dx+1) << 2 | d2, built at compile time.
+struct FaceAdjacency {
+  uint8_t e[3][42];
+};
+constexpr FaceAdjacency make_face_adjacency() {
+  FaceAdjacency t{};
+  for (int dd = 0; dd < 3; ++dd) {
+    int k = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx)
+          for (int d2 = 0; d2 < 3; ++d2) {
+            const int Dx = 2 * dx + (d2 == 0) - (dd == 0);
+            const int Dy = 2 * dy + (d2 == 1) - (dd == 1);
+            const int Dz = 2 * dz + (d2 == 2) - (dd == 2);
+            if (Dx * Dx + Dy * Dy + Dz * Dz > 8) continue;
+            if (dx == 0 && dy == 0 && dz == 0 && d2 == dd) continue;
+            t.e[dd][k++] = (uint8_t)(((dz + 1) << 6) | ((dy + 1) << 4) | ((dx + 1) << 2) | d2);
+          }
+  }
+  return t;
+}
+__constant__ FaceAdjacency kFaceAdj = make_face_adjacency();
+
+// Visits every interface face of the same pair adjacent to face (c, dd) over the 27 wrapped
+// neighbour cells, calling fn(k2, is_core): a walk over the table, not a test of all 81
+// (cell, direction) candidates.
 template <class Fn>
 __device__ __forceinline__ void for_adjacent_faces(Dims d, const FaceIndex& fx, long long f,
                                                    unsigned long long pk, Fn fn) {
@@ -384,24 +410,26 @@ __device__ __forceinline__ void for_adjacent_faces(Dims d, const FaceIndex& fx, 
   const long long c = f / 3;
   const int dd = (int)(f % 3);
   const int3 q = coords_of(c, nx, ny);
-  for (int dz = -1; dz <= 1; ++dz)
-    for (int dy = -1; dy <= 1; ++dy)
-      for (int dx = -1; dx <= 1; ++dx) {
-        const long long c2 =
-            ((long long)wrap1(q.z + dz, nz) * ny + wrap1(q.y + dy, ny)) * nx + wrap1(q.x + dx, nx);
-        for (int d2 = 0; d2 < 3; ++d2) {
-          const long long f2 = 3 * c2 + d2;
-          if (f2 == f) continue;
-          const int Dx = 2 * dx + (d2 == 0) - (dd == 0);
-          const int Dy = 2 * dy + (d2 == 1) - (dd == 1);
-          const int Dz = 2 * dz + (d2 == 2) - (dd == 2);
-          if (Dx * Dx + Dy * Dy + Dz * Dz > 8) continue;
-          if (!bitmap_test(fx.ifbits, f2)) continue;
-          const unsigned k2 = bitmap_rank(fx.ifbits, fx.ifpref, f2);
-          if (fx.fpair[k2] != pk) continue;
-          fn(k2, bitmap_test(fx.corebits, f2));
-        }
-      }
+  const int xm = wrap1(q.x - 1, nx), xp = wrap1(q.x + 1, nx);
+  const long long ym = (long long)wrap1(q.y - 1, ny) * nx, y0 = (long long)q.y * nx,
+                  yp = (long long)wrap1(q.y + 1, ny) * nx;
+  const long long plane = (long long)nx * ny;
+  const long long zm = wrap1(q.z - 1, nz) * plane, z0 = q.z * plane,
+                  zp = wrap1(q.z + 1, nz) * plane;
+#pragma unroll 1
+  for (int i = 0; i < 42; ++i) {
+    const unsigned e = kFaceAdj.e[dd][i];
+    const unsigned ez = e >> 6, ey = (e >> 4) & 3u, ex = (e >> 2) & 3u, d2 = e & 3u;
+    const long long c2 = (ez == 0 ? zm : (ez == 1 ? z0 : zp)) +
+                         (ey == 0 ? ym : (ey == 1 ? y0 : yp)) +
+                         (ex == 0 ? xm : (ex == 1 ? q.x : xp));
+    const long long f2 = 3 * c2 + d2;
+    if (f2 == f) continue;  // a wrapped copy of the face itself (an axis of 1 or 2 cells)
+    if (!bitmap_test(fx.ifbits, f2)) continue;
+    const unsigned k2 = bitmap_rank(fx.ifbits, fx.ifpref, f2);
+    if (fx.fpair[k2] != pk) continue;
+    fn(k2, bitmap_test(fx.corebits, f2));
+  }
 }
 
 // Tier unions: core faces with adjacent core faces (core CCL, :699-756) and film faces with
