@@ -906,8 +906,9 @@ __global__ void __launch_bounds__(STX* STY)
       }
     }
     if (z + 1 < z1) {  // warp-uniform
+      // a row whose ids all repeat the plane below keeps its labels
+      if (!__all_sync(0xffffffffu, kz == kc)) cur = lab.labels_warp(kz, in);
       kc = kz;
-      cur = lab.labels_warp(kz, in);
     }
   }
   if (want_pairs && !Lab::kKeyPairs) {

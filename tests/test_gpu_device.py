@@ -59,6 +59,28 @@ def test_pore_network_device_matches_oracle(gpu, port, torch, case):
     assert torch.equal(seg2, seg)
 
 
+def test_pore_network_device_on_a_side_stream(gpu, torch):
+    """The pore records run on the context's second stream: on a caller stream that is not the
+    default one, synchronising that stream alone must leave every output complete, and a
+    launch queued on it right after the call (a copy of the records) must see them."""
+    pnm, _ = gpu
+    from peclet_pnm_gb300 import device
+    from peclet_pnm_gb300 import synthetic as syn
+
+    sdf = syn.packing((64, 72, 80), 0.4, seed=9)
+    hp, hs, hq = pnm.extract_pore_network(sdf, [0, 0, 0], [1, 1, 1], numpy=True)
+    d = torch.from_numpy(sdf).cuda()
+    caller = torch.cuda.Stream()
+    for _ in range(3):
+        with torch.cuda.stream(caller):
+            pores, seg, pairs = device.extract_pore_network_device(d, [0, 0, 0], [1, 1, 1])
+            copied = pores.clone()  # queued on the caller's stream behind the call
+        caller.synchronize()
+        assert np.array_equal(copied.cpu().numpy(), hp)
+        assert np.array_equal(seg.cpu().numpy().reshape(-1), hs)
+        assert np.array_equal(pairs.cpu().numpy(), hq)
+
+
 @pytest.mark.parametrize("caps", [(1, 1), (1, 10 ** 6), (10 ** 6, 1)])
 def test_pore_network_device_capacity_retry(gpu, torch, caps):
     """Outputs smaller than the result: the call reports the counts and is re-run."""
