@@ -204,6 +204,7 @@ struct SegState {
   uint32_t* peakbits = nullptr; // bitmap of extract_pores peaks
   uint32_t* mbits = nullptr;    // marker bitmap, one word per 32-voxel row chunk
   long long n_words = 0;
+  bool ccl_done = false;        // the marker links were made during the SDF pass (host upload)
   unsigned n_edges = 0;         // marker-CCL links united
   int n_pore_labels = 0;        // np
   int n_solid_labels = 0;
@@ -238,8 +239,9 @@ void launch_pores_emit(const float* sdf, Dims d, const uint32_t* bits, const uns
 // Peak voxel ids of the pore records (voxel order, <= cap written; the count in *n_peaks).
 Status run_peak_ids(Ctx& c, const SegState& st, int32_t* d_out, int64_t cap, int64_t* n_peaks);
 // SDF pass only (for extract_pores alone).
+// ccl_in_slabs: with a host upload, make the marker links slab by slab behind the SDF pass.
 Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st,
-                    bool all_ascent = false, HostXfer* xfer = nullptr);
+                    bool all_ascent = false, HostXfer* xfer = nullptr, bool ccl_in_slabs = false);
 
 // ---- network flow (pnm_flow.cu) ------------------------------------------------------------
 struct FlowInputs {

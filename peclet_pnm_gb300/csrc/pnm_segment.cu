@@ -318,10 +318,11 @@ __device__ __forceinline__ int ccl_node_at(const uint32_t* __restrict__ vb, int 
 template <class G>
 __global__ void __launch_bounds__(256)
     k_ccl_words(G geo, const uint32_t* __restrict__ mbits, long long n_words, int* L,
-                unsigned* cnt) {
+                unsigned* cnt, long long w_begin = 0) {
+  // words [w_begin, n_words): a z-slab's words when the links are made slab by slab
   unsigned* err = &cnt[CNT_ERR];
   unsigned links = 0;
-  for (long long wi = (long long)blockIdx.x * blockDim.x + threadIdx.x; wi < n_words;
+  for (long long wi = w_begin + (long long)blockIdx.x * blockDim.x + threadIdx.x; wi < n_words;
        wi += (long long)gridDim.x * blockDim.x) {
     const uint32_t m = __ldg(&mbits[wi]);
     if (!m) continue;
@@ -1233,7 +1234,7 @@ int xfer_slab_planes(int nz) {
 }
 
 Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], SegState* st,
-                    bool all_ascent, HostXfer* xfer) {
+                    bool all_ascent, HostXfer* xfer, bool ccl_in_slabs) {
   const long long n = d.n();
   const long long words = (n + 31) / 32;
   StageScope stage(c, PNM_STAGE_SDF_PASS, "pnm::extract_pores+init_markers");
@@ -1285,11 +1286,28 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
       xfer->extra_done = c.events[2 * k + 1];
     }
     const long long tpp = (long long)((d.nx + TX - 1) / TX) * ((d.ny + TY - 1) / TY);
+    // With ccl_in_slabs, the marker links of slab i are made once slab i+1 has had its SDF pass
+    // (a word's forward rows reach one plane up), while later slabs are still uploading; the
+    // last slab's links (wrapping to plane 0) follow the loop.
+    const long long wpp = (long long)d.ny * ((d.nx + 31) / 32);  // bitmap words per plane
+    const OneVol cgeo{d, geo.thr};
+    auto ccl_slab = [&](int j) {
+      StageScope stage(c, PNM_STAGE_MERGE_MARKERS, "pnm::merge_markers");
+      const int a = j * zs, b = std::min(d.nz, a + zs);
+      k_ccl_words<<<grid_for((b - a) * wpp, 256, c.sm_count, PLAIN_GRID_PER_SM), 256, 0,
+                    c.stream>>>(cgeo, st->mbits, b * wpp, L, c.d_cnt, a * wpp);
+      ++c.launches;
+    };
     for (int i = 0; i < k; ++i) {
       const int z0 = i * zs, z1 = std::min(d.nz, z0 + zs);
       PNM_CUDA(cudaStreamWaitEvent(c.stream, c.events[std::min(i + 1, k - 1)], 0));
       geo.base = (int)(z0 / TZ_PLAIN * tpp);
       launch((unsigned)(((z1 - z0 + TZ_PLAIN - 1) / TZ_PLAIN) * tpp));
+      if (ccl_in_slabs && i > 0) ccl_slab(i - 1);
+    }
+    if (ccl_in_slabs) {
+      ccl_slab(k - 1);
+      st->ccl_done = true;
     }
   }
   PNM_CUDA(cudaGetLastError());
@@ -1303,7 +1321,7 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   const long long words = (n + 31) / 32;
   cudaStream_t s = c.stream;
   PNM_CUDA(cudaMemsetAsync(c.d_cnt, 0, CNT_COUNT * sizeof(unsigned), s));
-  PNM_TRY(run_sdf_pass(c, d_sdf, d, spacing, st, all_ascent, xfer));
+  PNM_TRY(run_sdf_pass(c, d_sdf, d, spacing, st, all_ascent, xfer, /*ccl_in_slabs=*/true));
   if (after_sdf) PNM_TRY((*after_sdf)());
   const OneVol geo{d, marker_threshold(spacing)};
   int* L = st->idtab;
@@ -1317,7 +1335,7 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   st->key = key;
   const unsigned tiles = (unsigned)boxes_of(d, TX, TY, TZ_PLAIN);
 
-  {
+  if (!st->ccl_done) {  // (a host upload made the links slab by slab behind it)
     StageScope stage(c, PNM_STAGE_MERGE_MARKERS, "pnm::merge_markers");
     k_ccl_words<<<grid_for(st->n_words, 256, c.sm_count, PLAIN_GRID_PER_SM), 256, 0, s>>>(
         geo, st->mbits, st->n_words, L, c.d_cnt);
