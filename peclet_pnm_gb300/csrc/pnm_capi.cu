@@ -221,6 +221,15 @@ T* host_dup(const T* src, size_t count) {
   return p;
 }
 
+// Waits for the context's host copies when the call's scope ends (early returns included), so
+// no copy still reads or writes a caller's host buffer after the call returns.
+struct CopyDrain {
+  Ctx& c;
+  ~CopyDrain() {
+    if (c.copy_stream) cudaStreamSynchronize(c.copy_stream);
+  }
+};
+
 Status upload_sdf(Ctx& c, const float* sdf, Dims d, const float** d_sdf) {
   float* buf = nullptr;
   PNM_TRY(c.buf(pnm::S_SDF, d.n(), &buf));
@@ -417,6 +426,7 @@ int pnm_segment_volume(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t ny, i
     int64_t dummy = 0;
     int32_t* dp = nullptr;
     pnm::HostXfer xfer;
+    CopyDrain drain{c};
     xfer.h_sdf = sdf;
     xfer.h_seg = seg;
     PNM_TRY(do_network(c, d_sdf, d, spacing_xyz, spacing_xyz, nullptr, 0, &dummy, d_seg, false,
@@ -539,6 +549,7 @@ int pnm_extract_pore_network(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t
     int32_t* d_pairs = nullptr;
     // the SDF goes up and the labels come back in z-slabs, overlapped with the pipeline
     pnm::HostXfer xfer;
+    CopyDrain drain{c};
     xfer.h_sdf = sdf;
     xfer.h_seg = seg;
     PNM_TRY(do_network(c, d_sdf, d, origin_xyz, spacing_xyz, d_pores, kMaxPores, &np, d_seg, true,
@@ -631,19 +642,22 @@ int pnm_extract_network_flow(pnm_ctx* ctx, const float* sdf, int32_t nx, int32_t
     const int slots[7] = {pnm::S_U, pnm::S_V, pnm::S_W, pnm::S_P, pnm::S_OX, pnm::S_OY, pnm::S_OZ};
     double* df[7] = {};
     // the SDF goes up in slabs ahead of the SDF pass; the fields follow on the copy stream and
-    // arrive while the segmentation runs (only the flow stage reads them)
+    // arrive while the segmentation runs: openness and velocities first (the face stages wait
+    // for them), the pressure last (only the pore pressures and throat dp read it)
     pnm::HostXfer xfer;
+    CopyDrain drain{c};
     xfer.h_sdf = sdf;
-    for (int i = 0; i < 7; ++i) {
+    for (int i : {4, 5, 6, 0, 1, 2, 3}) {
       if (!hf[i]) continue;
       PNM_TRY(c.buf(slots[i], d.n(), &df[i]));
       xfer.extra.push_back({df[i], hf[i], nb});
     }
     pnm::SegState st;
     PNM_TRY(pnm::run_segmentation(c, d_sdf, d, spacing_xyz, &st, /*all_ascent=*/true, &xfer));
-    if (xfer.extra_done) PNM_CUDA(cudaStreamWaitEvent(c.stream, xfer.extra_done, 0));
     pnm::FlowInputs in{df[0], df[1], df[2], df[3], df[4], df[5], df[6],
                        {grad_p_xyz[0], grad_p_xyz[1], grad_p_xyz[2]}};
+    in.fields_ready = xfer.extra_early;
+    in.p_ready = xfer.extra_done;
     pnm::FlowOutputsDev od;
     PNM_TRY(pnm::run_network_flow(c, st, origin_xyz, spacing_xyz, in, &od));
     pnm::FlowOutputsHost o;

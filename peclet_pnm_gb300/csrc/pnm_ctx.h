@@ -174,6 +174,7 @@ struct HostXfer {
   };
   std::vector<Copy> extra;
   cudaEvent_t extra_done = nullptr;
+  cudaEvent_t extra_early = nullptr;  // after every extra copy but the last (two or more)
 };
 // z-planes per transfer slab (a multiple of 16, the tile and brick depth) for nz planes
 int xfer_slab_planes(int nz);
@@ -247,6 +248,8 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
 struct FlowInputs {
   const double *u, *v, *w, *p, *ox, *oy, *oz;  // device pointers; o* may be null
   double grad_p[3];
+  // host uploads still in flight (null: resident): the velocities and openness, and p
+  cudaEvent_t fields_ready = nullptr, p_ready = nullptr;
 };
 struct FlowOutputsHost {
   std::vector<pnm_pore> pores;

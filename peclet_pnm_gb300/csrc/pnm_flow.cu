@@ -770,8 +770,6 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
     geo.o[a] = origin[a];
     geo.s[a] = spacing[a];
   }
-  k_centers_pressure<<<gridn(np, c.sm_count), 256, 0, s>>>(st.sdf, d, geo, peak, np, in.p, pores,
-                                                           ppres); ++c.launches;
   k_flow_basins<<<gridn(n, c.sm_count), 256, 0, s>>>(d, st.code, st.nxt, st.key, seg, flowLab); ++c.launches;
   PNM_CUDA(cudaGetLastError());
 
@@ -790,6 +788,7 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
   const double Ax = (double)spacing[1] * spacing[2], Ay = (double)spacing[0] * spacing[2],
                Az = (double)spacing[0] * spacing[1];  // :869-870
   const FieldPtrs fp{in.u, in.v, in.w, in.ox, in.oy, in.oz};
+  if (in.fields_ready) PNM_CUDA(cudaStreamWaitEvent(s, in.fields_ready, 0));
   k_face_class<<<gridn(n, c.sm_count), 256, 0, s>>>(d, st.code, flowLab, fp, Ax, Ay, Az, ifbits,
                                                      corebits, bounds); ++c.launches;
   exclusive_scan(PopcountOf{ifbits}, fwords, ifpref, scan0, s, &c.launches);
@@ -905,6 +904,11 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
   unsigned long long* accCx = accA + 2 * ntx;
   unsigned long long* accCy = accCx + 2 * ntx;
   unsigned long long* accCz = accCy + 2 * ntx;
+  // pore centres and pressures: the pressure field is the last host upload
+  if (in.p_ready) PNM_CUDA(cudaStreamWaitEvent(s, in.p_ready, 0));
+  k_centers_pressure<<<gridn(np, c.sm_count), 256, 0, s>>>(st.sdf, d, geo, peak, np, in.p, pores,
+                                                           ppres);
+  ++c.launches;
   k_flux_resid<<<gridn(n, c.sm_count), 256, 0, s>>>(d, flowLab, fp, P, accR); ++c.launches;
   if (M > 0 && nt > 0) {
     k_flux_throats<<<gridn(M, c.sm_count), 256, 0, s>>>(d, M, fid, flowLab, fp, label, slotOf,

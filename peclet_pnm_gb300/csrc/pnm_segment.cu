@@ -1266,7 +1266,7 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
     const int zs = xfer_slab_planes(d.nz), k = (d.nz + zs - 1) / zs;
     const long long plane = (long long)d.nx * d.ny;
     float* dst = const_cast<float*>(d_sdf);
-    PNM_TRY(c.ensure_copy_events(2 * k + 2));
+    PNM_TRY(c.ensure_copy_events(2 * k + 3));
     PNM_CUDA(cudaEventRecord(c.events[2 * k], c.stream));  // the device buffer is free
     PNM_CUDA(cudaStreamWaitEvent(c.copy_stream, c.events[2 * k], 0));
     PNM_CUDA(cudaMemcpyAsync(dst + (d.nz - 1) * plane, xfer->h_sdf + (d.nz - 1) * plane,
@@ -1279,9 +1279,15 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
       PNM_CUDA(cudaEventRecord(c.events[i], c.copy_stream));
     }
     if (!xfer->extra.empty()) {
-      for (const auto& cp : xfer->extra)
+      for (size_t j = 0; j < xfer->extra.size(); ++j) {
+        const auto& cp = xfer->extra[j];
+        if (j + 1 == xfer->extra.size() && j > 0) {
+          PNM_CUDA(cudaEventRecord(c.events[2 * k + 2], c.copy_stream));
+          xfer->extra_early = c.events[2 * k + 2];
+        }
         PNM_CUDA(cudaMemcpyAsync(cp.dst, cp.src, cp.bytes, cudaMemcpyHostToDevice,
                                  c.copy_stream));
+      }
       PNM_CUDA(cudaEventRecord(c.events[2 * k + 1], c.copy_stream));
       xfer->extra_done = c.events[2 * k + 1];
     }
