@@ -57,7 +57,6 @@ enum Counter : int {
   CNT_SWEEPS,        // flood sweeps run by the persistent flood loop
   CNT_BAR0,          // grid barrier of the persistent flood loop: arrivals
   CNT_BAR1,          //   and generation
-  CNT_GATHER,        // hash slots gathered so far (append order)
   CNT_COUNT = 32
 };
 

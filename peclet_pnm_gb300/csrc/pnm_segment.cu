@@ -931,15 +931,13 @@ struct Occupied {
 };
 
 // Gathers the occupied hash slots into dense keys re-encoded as (lo - base) << b | (hi - base):
-// at their rank among the occupied slots (pos); or, with `fill` (a zeroed counter), appended in
-// any order (the keys are sorted next); or, with neither, in place (a dense key list).
-__device__ __forceinline__ long long gather_slot(long long i, const unsigned* pos,
-                                                 unsigned* fill) {
-  return fill ? (long long)warp_append(fill, true) : (pos ? (long long)pos[i] : i);
+// at their rank among the occupied slots (pos), or in place (pos == nullptr: a dense key list).
+__device__ __forceinline__ long long gather_slot(long long i, const unsigned* pos) {
+  return pos ? (long long)pos[i] : i;
 }
 __global__ void k_hash_gather(const unsigned long long* __restrict__ table, long long cap,
-                              const unsigned* __restrict__ pos, unsigned* fill, const int* range,
-                              int b, uint64_t* __restrict__ keys) {
+                              const unsigned* __restrict__ pos, const int* range, int b,
+                              uint64_t* __restrict__ keys) {
   const int base = range[0];
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cap;
        i += (long long)gridDim.x * blockDim.x) {
@@ -948,7 +946,7 @@ __global__ void k_hash_gather(const unsigned long long* __restrict__ table, long
     const int lo = (int)((uint32_t)(k >> 32) ^ 0x80000000u);
     const int hi = (int)((uint32_t)k ^ 0x80000000u);
     const uint32_t dlo = (uint32_t)lo - (uint32_t)base, dhi = (uint32_t)hi - (uint32_t)base;
-    keys[gather_slot(i, pos, fill)] = ((uint64_t)dlo << b) | (uint64_t)dhi;
+    keys[gather_slot(i, pos)] = ((uint64_t)dlo << b) | (uint64_t)dhi;
   }
 }
 
@@ -958,7 +956,7 @@ __global__ void k_hash_gather(const unsigned long long* __restrict__ table, long
 // its own volume). Then re-encoded as (lo - base) << b | (hi - base) like k_hash_gather.
 template <class G>
 __global__ void k_hash_gather_keys(const unsigned long long* __restrict__ table, long long cap,
-                                   const unsigned* __restrict__ pos, unsigned* fill, G geo,
+                                   const unsigned* __restrict__ pos, G geo,
                                    const int* __restrict__ L, const int* range, int b,
                                    uint64_t* __restrict__ keys) {
   const int base = range[0];
@@ -975,7 +973,7 @@ __global__ void k_hash_gather_keys(const unsigned long long* __restrict__ table,
     const int la = gb + label_of_key(L, ka), lb = gb + label_of_key(L, kb);
     const int lo = min(la, lb), hi = max(la, lb);
     const uint32_t dlo = (uint32_t)lo - (uint32_t)base, dhi = (uint32_t)hi - (uint32_t)base;
-    keys[gather_slot(i, pos, fill)] = ((uint64_t)dlo << b) | (uint64_t)dhi;
+    keys[gather_slot(i, pos)] = ((uint64_t)dlo << b) | (uint64_t)dhi;
   }
 }
 
@@ -1521,11 +1519,10 @@ Status emit_pairs(Ctx& c, Dims d, bool from_keys, const SegState* st, const int3
     PNM_TRY(c.buf(S_RSHIST, 256 * (m / RS_TILE + 1) + 1, &hist));
     // the m keys the inserts appended (no sweep of the set)
     if (from_keys)
-      k_hash_gather_keys<<<grid_for(m, 256, c.sm_count), 256, 0, s>>>(
-          dense, m, nullptr, nullptr, geo, st->idtab, range, b, ka);
+      k_hash_gather_keys<<<grid_for(m, 256, c.sm_count), 256, 0, s>>>(dense, m, nullptr, geo,
+                                                                      st->idtab, range, b, ka);
     else
-      k_hash_gather<<<grid_for(m, 256, c.sm_count), 256, 0, s>>>(dense, m, nullptr, nullptr,
-                                                                 range, b, ka);
+      k_hash_gather<<<grid_for(m, 256, c.sm_count), 256, 0, s>>>(dense, m, nullptr, range, b, ka);
     ++c.launches;
     const bool in_b = radix_sort(ka, nullptr, kb, nullptr, m, 0, 2 * b, hist, scan0, s, &c.launches);
     k_pairs_decode<<<grid_for(m, 256, c.sm_count), 256, 0, s>>>(in_b ? kb : ka, m, range, b, out); ++c.launches;
@@ -1690,8 +1687,8 @@ Status enqueue_batch(BatchPlan& p, cudaStream_t s, long long* launches) {
   exclusive_scan(Occupied{p.table}, p.hash_cap, p.hpos, p.scan_tmp, s, launches);
   const unsigned* m_p = p.hpos + p.hash_cap;
   const unsigned hgrid = grid_for(p.hash_cap, 256, sm);
-  k_hash_gather_keys<<<hgrid, 256, 0, s>>>(p.table, p.hash_cap, p.hpos, nullptr, geo, p.L,
-                                           p.range, p.label_bits, p.ka);
+  k_hash_gather_keys<<<hgrid, 256, 0, s>>>(p.table, p.hash_cap, p.hpos, geo, p.L, p.range,
+                                           p.label_bits, p.ka);
   p.pairs_in_b = radix_sort(p.ka, nullptr, p.kb, nullptr, p.hash_cap, 0, 2 * p.label_bits, p.hist,
                             p.scan_tmp, s, launches, m_p);
   const uint64_t* sorted = p.pairs_in_b ? p.kb : p.ka;
