@@ -559,12 +559,14 @@ __global__ void __launch_bounds__(TX* TY, 8)
   }
 }
 
-// layer 2: listed flood voxels with a seed neighbour (they have no marker neighbour)
+// Layer 2 with its labels: a listed flood voxel (no marker neighbour) with a seed neighbour joins
+// the layer, and its sweep-2 label is already known here: the neighbours labelled before sweep 2
+// are the seeds alone (solid keys; the other flood voxels hold KEY_NONE or PENDING, pores their
+// basin roots), so the flood loop starts by publishing these labels.
 template <class G>
 __global__ void __launch_bounds__(256)
-    k_flood_layer2(G geo, const uint8_t* __restrict__ code, int* key,
-                   const int* __restrict__ ulist, const unsigned* nu_p, int* __restrict__ fout,
-                   unsigned* nout_p) {
+    k_flood_layer2(G geo, int* key, const int* __restrict__ ulist, const unsigned* nu_p,
+                   int* __restrict__ fout, int* __restrict__ tmp, unsigned* nout_p) {
   const unsigned nu = *nu_p;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nu;
        i += (long long)gridDim.x * blockDim.x) {
@@ -573,22 +575,21 @@ __global__ void __launch_bounds__(256)
     geo.locate(v, off, nx, ny, nz);
     const int lv = v - off;
     const int x = lv % nx, y = (lv / nx) % ny, z = lv / (nx * ny);
-    bool hit = false;
-    for (int dz = -1; dz <= 1 && !hit; ++dz)
-      for (int dy = -1; dy <= 1 && !hit; ++dy)
+    int bestk = INT_MIN;
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
         for (int dx = -1; dx <= 1; ++dx) {
           if (!dx && !dy && !dz) continue;
           const int u =
               off + (wrap1(z + dz, nz) * ny + wrap1(y + dy, ny)) * nx + wrap1(x + dx, nx);
-          const uint8_t cu = __ldg(&code[u]);
-          if (code_cls(cu) == CLS_FLOOD && code_seed(cu)) {
-            hit = true;
-            break;
-          }
+          const int k = key[u];
+          if (key_is_solid(k)) bestk = max(bestk, k);
         }
-    if (hit) {
+    if (bestk != INT_MIN) {
       key[v] = KEY_PENDING;
-      fout[atomicAdd(nout_p, 1u)] = v;
+      const unsigned pos = atomicAdd(nout_p, 1u);
+      fout[pos] = v;
+      tmp[pos] = ~bestk;
     }
   }
 }
@@ -670,6 +671,8 @@ __global__ void __launch_bounds__(256)
     k_flood_loop(G geo, const uint8_t* __restrict__ code, int* key, int* L, int* fa, int* fb,
                  int* tmp, unsigned* cnt, int max_sweeps, unsigned long long wait_ns,
                  unsigned wait_extra) {
+  // the first layer (k_flood_layer2's) arrives with its labels in tmp and an empty (zeroed)
+  // next-layer counter, so the first sweep starts at publishing
   unsigned* err = &cnt[CNT_ERR];
   unsigned* bar = &cnt[CNT_BAR0];
   int* fin = fa;
@@ -692,10 +695,12 @@ __global__ void __launch_bounds__(256)
     __syncthreads();
     const unsigned nin = s_nin;
     if (s_stop) break;
-    for (long long i = tid; i < nin; i += stride)
-      tmp[i] = flood_assign_one<true>(geo, key, __ldcg(&fin[i]));
-    if (tid == 0) atomicExch(&cnt[cout], 0u);  // read by nobody since the last barrier
-    if (!grid_barrier(bar, err, wait_ns, wait_extra)) break;
+    if (sweeps > 1) {
+      for (long long i = tid; i < nin; i += stride)
+        tmp[i] = flood_assign_one<true>(geo, key, __ldcg(&fin[i]));
+      if (tid == 0) atomicExch(&cnt[cout], 0u);  // read by nobody since the last barrier
+      if (!grid_barrier(bar, err, wait_ns, wait_extra)) break;
+    }
     for (long long i = tid; i < nin; i += stride)
       flood_discover_one(geo, code, key, L, __ldcg(&fin[i]), __ldcg(&tmp[i]), fout, &cnt[cout]);
     if (!grid_barrier(bar, err, wait_ns, wait_extra)) break;
@@ -1355,7 +1360,7 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
   StageScope flood_stage(c, PNM_STAGE_FLOOD, "pnm::flood");
   k_flood_seed<OneVol, TZ_PLAIN><<<tiles, TX * TY, 0, s>>>(geo, st->code, key, L, ulist, c.d_cnt);
   const unsigned fgrid = grid_for(n, 256, c.sm_count, 4);
-  k_flood_layer2<<<fgrid, 256, 0, s>>>(geo, st->code, key, ulist, &c.d_cnt[CNT_ULIST], f0,
+  k_flood_layer2<<<fgrid, 256, 0, s>>>(geo, key, ulist, &c.d_cnt[CNT_ULIST], f0, tmp,
                                        &c.d_cnt[CNT_FRONT0]);
   c.launches += 2;
   PNM_CUDA(cudaGetLastError());
@@ -1377,10 +1382,13 @@ Status run_segmentation(Ctx& c, const float* d_sdf, Dims d, const float spacing[
     while (true) {
       for (int b = 0; b < kBatch; ++b) {
         PNM_CUDA(cudaMemsetAsync(&c.d_cnt[cout], 0, sizeof(unsigned), s));
-        k_flood_assign<<<fgrid, 256, 0, s>>>(geo, key, fin, &c.d_cnt[cin], tmp);
+        if (sweeps > 1) {  // the first layer's labels came with it (k_flood_layer2)
+          k_flood_assign<<<fgrid, 256, 0, s>>>(geo, key, fin, &c.d_cnt[cin], tmp);
+          ++c.launches;
+        }
         k_flood_discover<<<fgrid, 256, 0, s>>>(geo, st->code, key, L, fin, &c.d_cnt[cin], tmp,
                                                fout, &c.d_cnt[cout]);
-        c.launches += 2;
+        ++c.launches;
         std::swap(fin, fout);
         std::swap(cin, cout);
         ++sweeps;
@@ -1665,7 +1673,7 @@ Status enqueue_batch(BatchPlan& p, cudaStream_t s, long long* launches) {
       k_flood_seed<VolTab, 8><<<tiles, TX * TY, 0, s>>>(geo, p.code, p.key, p.L, p.ulist, p.cnt);
   }
   k_flood_layer2<<<grid_for(n, 256, sm, 4), 256, 0, s>>>(
-      geo, p.code, p.key, p.ulist, &p.cnt[CNT_ULIST], p.f0, &p.cnt[CNT_FRONT0]);
+      geo, p.key, p.ulist, &p.cnt[CNT_ULIST], p.f0, p.tmp, &p.cnt[CNT_FRONT0]);
   *launches += 6;
   PNM_CUDA(cudaGetLastError());
   PNM_CUDA(launch_flood_loop(geo, p.code, p.key, p.L, p.f0, p.f1, p.tmp, p.cnt, p.max_sweeps, sm,
