@@ -105,8 +105,14 @@ __global__ void __launch_bounds__(TX* TY, 8)  // 8 resident tiles per SM (32 reg
   if (t < HY) wy[t] = ((Y0 - 1 + t) % ny + ny) % ny;
   if (t < HZ) wz[t] = ((Z0 - 1 + t) % nz + nz) % nz;
   __syncthreads();
-  for (int r = t >> 5; r < HY * HZ; r += NT / 32) {  // halo rows and their marker masks
-    const int hy = r % HY, hz = r / HY;
+  static_assert(NT / 32 < HY, "a warp steps at most one halo plane per row iteration");
+  // halo rows and their marker masks: warp w takes rows w, w + 8, ... (plane-major)
+  for (int hy = t >> 5, hz = 0; hz < HZ; hy += NT / 32) {
+    if (hy >= HY) {
+      hy -= HY;
+      ++hz;
+      if (hz >= HZ) break;
+    }
     const float* src = sdf + (wz[hz] * nxy + wy[hy] * nx);
     const float v0 = __ldg(&src[wx[lane + 1]]);
     so[hz][hy][lane + 1] = ord_key(v0);
