@@ -262,7 +262,12 @@ Status do_network(Ctx& c, const float* d_sdf, Dims d, const float* org, const fl
                   bool want_pairs, int32_t** d_pairs, int64_t* n_pairs,
                   pnm::HostXfer* xfer = nullptr) {
   pnm::SegState st;
-  // the pore records need the SDF pass alone: they run on the side stream meanwhile
+  // the pore records need the SDF pass alone: they run on the side stream meanwhile; the
+  // caller's stream joins it however the call ends, so later work there is ordered after it
+  struct SideJoin {
+    Ctx& c;
+    ~SideJoin() { (void)c.join_side(); }
+  } side_join{c};
   const std::function<Status()> pores = [&]() {
     return pnm::run_pores_side(c, st, org, spc, d_pores, pore_cap);
   };
