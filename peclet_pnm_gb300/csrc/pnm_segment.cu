@@ -23,7 +23,7 @@ namespace pnm {
 constexpr int TX = 32, TY = 8;  // SDF-pass tile: 32 x 8 x TZ voxels (TZ = 8 unless tuned), 256 threads
 // launch shape of the single-volume entry points (the batch path tunes its own)
 constexpr int TZ_PLAIN = 16;           // SDF-pass / flood-seed tile depth
-constexpr int PLAIN_GRID_PER_SM = 16;  // grid-stride stages: blocks per SM
+constexpr int PLAIN_GRID_PER_SM = 8;  // marker CCL: one wave of resident blocks per SM
 constexpr int PLAIN_FLOOD_PER_SM = 4;  // persistent flood loop: resident blocks per SM
 constexpr int kBig = INT_MAX;           // unset min-index / non-marker parent
 
