@@ -470,7 +470,7 @@ __global__ void k_face_flatten(long long M, const int* __restrict__ par, int* __
 // Film attachment: a film component takes the smallest core-patch root adjacent to any of its
 // faces — the fixpoint of the reference's min propagation through films (:763-805). Components
 // adjacent to no core keep their own minimum (the leftover tier, :807-818).
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 8)
     k_film_attach(Dims d, FaceIndex fx, const int* __restrict__ fid, long long M,
                   const int* __restrict__ par, int* __restrict__ minCore) {
   for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < M;
