@@ -718,6 +718,17 @@ __global__ void k_fill_int(int* p, long long m, int v) {
     p[i] = v;
 }
 
+// Blocks of 256 threads of `kernel` resident on one SM (its registers decide): grid-stride
+// kernels sized to one wave of them run without a partial second wave.
+template <class K>
+int resident_per_sm(K kernel) {
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, 256, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return 8;
+  }
+  return b < 1 ? 1 : b;
+}
 inline unsigned gridn(long long work, int sm_count, int per_sm = 8) {
   long long b = (work + 255) / 256;
   const long long cap = (long long)sm_count * per_sm;
@@ -789,8 +800,9 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
                Az = (double)spacing[0] * spacing[1];  // :869-870
   const FieldPtrs fp{in.u, in.v, in.w, in.ox, in.oy, in.oz};
   if (in.fields_ready) PNM_CUDA(cudaStreamWaitEvent(s, in.fields_ready, 0));
-  k_face_class<<<gridn(n, c.sm_count), 256, 0, s>>>(d, st.code, flowLab, fp, Ax, Ay, Az, ifbits,
-                                                     corebits, bounds); ++c.launches;
+  k_face_class<<<gridn(n, c.sm_count, resident_per_sm(k_face_class)), 256, 0, s>>>(
+      d, st.code, flowLab, fp, Ax, Ay, Az, ifbits, corebits, bounds);
+  ++c.launches;
   exclusive_scan(PopcountOf{ifbits}, fwords, ifpref, scan0, s, &c.launches);
   PNM_CUDA(cudaGetLastError());
   unsigned M32 = 0;
@@ -909,10 +921,12 @@ Status run_network_flow(Ctx& c, const SegState& st, const float origin[3], const
   k_centers_pressure<<<gridn(np, c.sm_count), 256, 0, s>>>(st.sdf, d, geo, peak, np, in.p, pores,
                                                            ppres);
   ++c.launches;
-  k_flux_resid<<<gridn(n, c.sm_count), 256, 0, s>>>(d, flowLab, fp, P, accR); ++c.launches;
+  k_flux_resid<<<gridn(n, c.sm_count, resident_per_sm(k_flux_resid)), 256, 0, s>>>(d, flowLab, fp,
+                                                                                  P, accR);
+  ++c.launches;
   if (M > 0 && nt > 0) {
-    k_flux_throats<<<gridn(M, c.sm_count), 256, 0, s>>>(d, M, fid, flowLab, fp, label, slotOf,
-                                                         peak, P, accQ, accA, accCx, accCy, accCz);
+    k_flux_throats<<<gridn(M, c.sm_count, resident_per_sm(k_flux_throats)), 256, 0, s>>>(
+        d, M, fid, flowLab, fp, label, slotOf, peak, P, accQ, accA, accCx, accCy, accCz);
     ++c.launches;
   }
   double* dres;
