@@ -1238,7 +1238,7 @@ cudaError_t launch_flood_loop(G geo, const uint8_t* code, int* key, int* L, int*
 }  // namespace
 
 int xfer_slab_planes(int nz) {
-  const int k = std::max(1, std::min(8, (nz + 15) / 16));  // up to 8 slabs
+  const int k = std::max(1, std::min(16, (nz + 15) / 16));  // up to 16 slabs
   return ((nz + k - 1) / k + 15) / 16 * 16;
 }
 
@@ -1280,11 +1280,14 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
     PNM_CUDA(cudaStreamWaitEvent(c.copy_stream, c.events[2 * k], 0));
     PNM_CUDA(cudaMemcpyAsync(dst + (d.nz - 1) * plane, xfer->h_sdf + (d.nz - 1) * plane,
                              plane * sizeof(float), cudaMemcpyHostToDevice, c.copy_stream));
+    // copy i ends one plane into slab i+1 (and, for i > 0, starts one plane into slab i), so
+    // event i marks the arrival of every plane the SDF pass of slab i reads
     for (int i = 0; i < k; ++i) {
-      const int z0 = i * zs, z1 = std::min(d.nz, z0 + zs);
-      PNM_CUDA(cudaMemcpyAsync(dst + z0 * plane, xfer->h_sdf + z0 * plane,
-                               (z1 - z0) * plane * sizeof(float), cudaMemcpyHostToDevice,
-                               c.copy_stream));
+      const int a = i == 0 ? 0 : i * zs + 1, b = std::min(d.nz, (i + 1) * zs + 1);
+      if (b > a)
+        PNM_CUDA(cudaMemcpyAsync(dst + a * plane, xfer->h_sdf + a * plane,
+                                 (b - a) * plane * sizeof(float), cudaMemcpyHostToDevice,
+                                 c.copy_stream));
       PNM_CUDA(cudaEventRecord(c.events[i], c.copy_stream));
     }
     if (!xfer->extra.empty()) {
@@ -1315,7 +1318,7 @@ Status run_sdf_pass(Ctx& c, const float* d_sdf, Dims d, const float spacing[3], 
     };
     for (int i = 0; i < k; ++i) {
       const int z0 = i * zs, z1 = std::min(d.nz, z0 + zs);
-      PNM_CUDA(cudaStreamWaitEvent(c.stream, c.events[std::min(i + 1, k - 1)], 0));
+      PNM_CUDA(cudaStreamWaitEvent(c.stream, c.events[i], 0));
       geo.base = (int)(z0 / TZ_PLAIN * tpp);
       launch((unsigned)(((z1 - z0 + TZ_PLAIN - 1) / TZ_PLAIN) * tpp));
       if (ccl_in_slabs && i > 0) ccl_slab(i - 1);

@@ -62,6 +62,19 @@ def test_network_flow_matches_oracle(gpu, port, case, with_openness):
     _check(r, o)
 
 
+@pytest.mark.parametrize("nz", [33, 257])
+def test_flow_host_slab_boundaries(gpu, port, nz):
+    """The seven fields follow the SDF's z-slabs on the copy stream; at these depths the last
+    slab is one plane, already carried by the copy before it."""
+    pnm, _ = gpu
+    sdf = syn.packing((nz, 9, 11), 0.4, mean_r=3.0, seed=nz)
+    f = flow_fields(sdf)
+    gp = [1e-3, -2e-3, 5e-4]
+    kw = dict(ox=f[4], oy=f[5], oz=f[6])
+    r = pnm.extract_network_flow(sdf, [0] * 3, [1] * 3, *f[:4], grad_p_zyx=gp, numpy=True, **kw)
+    _check(r, port.extract_network_flow(sdf, [0] * 3, [1] * 3, *f[:4], grad_p_zyx=gp, **kw))
+
+
 def test_flow_goldens(gpu, port):
     pnm, _ = gpu
     from golden.make_golden import FLOW_CASES

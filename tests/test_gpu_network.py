@@ -107,6 +107,19 @@ def test_repeated_calls_are_identical_and_reuse_workspace(gpu):
         assert np.array_equal(x, y)
 
 
+@pytest.mark.parametrize("nz", [17, 33, 48, 257, 271])
+def test_host_slab_boundaries(gpu, port, nz):
+    """Host-buffer calls upload the SDF in z-slabs of 16-plane multiples, each copy ending one
+    plane into the next slab; these depths leave a last slab of one plane (nothing left to copy
+    for it), a ragged one, or an even split."""
+    pnm, _ = gpu
+    rng = np.random.default_rng(nz)
+    sdf = syn.packing((nz, 9, 11), 0.4, mean_r=3.0, seed=nz)
+    sdf += rng.normal(0.0, 0.05, size=sdf.shape).astype(np.float32)
+    out = pnm.extract_pore_network(sdf, [0] * 3, [1] * 3, numpy=True)
+    _check(out, port.extract_pore_network(sdf, [0] * 3, [1] * 3))
+
+
 @pytest.mark.slow
 def test_packing_128_matches_oracle(gpu, port):
     pnm, _ = gpu
