@@ -91,9 +91,16 @@ Status Ctx::join_side() {
   return Status::ok();
 }
 
+// The counters reach the host through a kernel's stores to mapped pinned memory: a copy-engine
+// transfer would queue behind label slabs already on their way to the host, and the pair stages
+// that wait for the pair count would then start only after the whole label download.
+__global__ void k_counters_to_host(const unsigned* __restrict__ d, unsigned* h) {
+  for (int i = threadIdx.x; i < CNT_COUNT; i += blockDim.x) h[i] = d[i];
+}
 Status Ctx::read_counters() {
-  PNM_CUDA(cudaMemcpyAsync(h_cnt, d_cnt, CNT_COUNT * sizeof(unsigned), cudaMemcpyDeviceToHost,
-                           stream));
+  k_counters_to_host<<<1, 32, 0, stream>>>(d_cnt, h_cnt_dev);
+  ++launches;
+  PNM_CUDA(cudaGetLastError());
   PNM_CUDA(cudaStreamSynchronize(stream));
   return Status::ok();
 }
@@ -307,7 +314,9 @@ int pnm_ctx_create(int device, pnm_ctx** out) {
   if (cudaSetDevice(device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMalloc(&c.d_cnt, pnm::CNT_COUNT * sizeof(unsigned)) != cudaSuccess ||
-      cudaMallocHost(&c.h_cnt, pnm::CNT_COUNT * sizeof(unsigned)) != cudaSuccess) {
+      cudaHostAlloc(&c.h_cnt, pnm::CNT_COUNT * sizeof(unsigned), cudaHostAllocMapped) !=
+          cudaSuccess ||
+      cudaHostGetDevicePointer(&c.h_cnt_dev, c.h_cnt, 0) != cudaSuccess) {
     cudaGetLastError();
     delete ctx;
     return PNM_ERR_CUDA;

@@ -92,7 +92,8 @@ struct Ctx {
   std::vector<cudaEvent_t> events;     // slab events of those transfers
   Workspace ws;
   unsigned* d_cnt = nullptr;  // CNT_COUNT device counters
-  unsigned* h_cnt = nullptr;  // pinned host mirror
+  unsigned* h_cnt = nullptr;      // pinned, mapped host mirror
+  unsigned* h_cnt_dev = nullptr;  // its device address
   int sm_count = 0;
   long long launches = 0;   // kernels launched by this context (cumulative)
   long long calls = 0;      // entry-point calls (cumulative)
@@ -139,7 +140,7 @@ struct Ctx {
     *out = static_cast<T*>(p);
     return s;
   }
-  Status read_counters();  // synchronises the stream and copies d_cnt -> h_cnt
+  Status read_counters();  // copies d_cnt -> h_cnt on the stream and synchronises it
   Status ensure_copy_events(int n);  // creates the copy stream and at least n events
 };
 
