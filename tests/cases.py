@@ -111,3 +111,24 @@ def flow_fields(sdf, seed=5):
         x = rng.uniform(-0.3, 1.0, size=sh)
         o.append(np.ascontiguousarray(np.clip(x, 0.0, 1.0)))
     return f + o
+
+
+def random_volume(seed):
+    """A seeded volume of random shape (1..20 per axis) from one of four value families: smooth
+    noise, values quantised to a few levels (plateaus and ties), a marker-heavy field and a
+    packing with noise; spacing anisotropic and origin offset at random."""
+    rng = np.random.default_rng(1000 + seed)
+    shp = tuple(int(v) for v in rng.integers(1, 21, size=3))
+    kind = seed % 4
+    if kind == 0:
+        a = rng.normal(0.0, 2.0, size=shp)
+    elif kind == 1:
+        a = np.round(rng.normal(0.0, 1.5, size=shp) * 2.0) / 2.0
+    elif kind == 2:
+        a = np.where(rng.random(shp) < 0.6, -3.0, rng.uniform(-1.0, 2.0, size=shp))
+    else:
+        a = syn.packing(tuple(max(4, s) for s in shp), 0.4, mean_r=2.5, seed=seed)
+        a = a + rng.normal(0.0, 0.1, size=a.shape)
+    spc = [float(v) for v in rng.uniform(0.5, 2.0, size=3)]
+    org = [float(v) for v in rng.uniform(-5.0, 5.0, size=3)]
+    return np.ascontiguousarray(a, dtype=np.float32), org, spc

@@ -8,7 +8,7 @@ import os
 import numpy as np
 import pytest
 
-from cases import edge_cases, standard_cases
+from cases import edge_cases, flow_fields, random_volume, standard_cases
 from oracle import sorted_pores
 from peclet_pnm_gb300 import synthetic as syn
 
@@ -105,6 +105,25 @@ def test_repeated_calls_are_identical_and_reuse_workspace(gpu):
     r2 = pnm.extract_pore_network(a, [0] * 3, [1] * 3, numpy=True)
     for x, y in zip(r1, r2):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_random_volumes_match_oracle(gpu, port, seed):
+    """Seeded volumes of random shape, value family, anisotropic spacing and origin (the oracle
+    equals the reference bitwise on the same volumes): the network bit-exact, and on every fifth
+    volume the network flow within the flow bar."""
+    pnm, _ = gpu
+    sdf, org, spc = random_volume(seed)
+    _check(pnm.extract_pore_network(sdf, org, spc, numpy=True),
+           port.extract_pore_network(sdf, org, spc))
+    if seed % 5 == 0 and sdf.size >= 8:
+        from test_gpu_flow import _check as check_flow
+
+        f = flow_fields(sdf)
+        kw = dict(ox=f[4], oy=f[5], oz=f[6])
+        gp = [2e-3, -1e-3, 5e-4]
+        check_flow(pnm.extract_network_flow(sdf, org, spc, *f[:4], grad_p_zyx=gp, numpy=True, **kw),
+                   port.extract_network_flow(sdf, org, spc, *f[:4], grad_p_zyx=gp, **kw))
 
 
 @pytest.mark.parametrize("nz", [17, 33, 48, 257, 271])

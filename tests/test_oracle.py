@@ -13,7 +13,7 @@ import os
 import numpy as np
 import pytest
 
-from cases import edge_cases, flow_fields, standard_cases
+from cases import edge_cases, flow_fields, random_volume, standard_cases
 from oracle import Oracle, reference_available, sorted_pores
 from peclet_pnm_gb300 import synthetic as syn
 
@@ -114,6 +114,31 @@ def test_port_flow_matches_reference_edge_cases(port, case):
         assert np.array_equal(a["pores"].view(np.int32), b["pores"].view(np.int32))
         for k in ("throat_flow", "throat_area", "pore_residual", "pore_pressure", "throat_dp"):
             assert np.array_equal(a[k], b[k]), k  # same serial order -> bitwise
+
+
+@needs_ref
+@pytest.mark.parametrize("seed", range(40))
+def test_port_matches_reference_random_volumes(port, seed):
+    sdf, org, spc = random_volume(seed)
+    ref = Oracle("reference")
+    a = ref.extract_pore_network(sdf, org, spc)
+    b = port.extract_pore_network(sdf, org, spc)
+    assert np.array_equal(a[1], b[1]), "seg"
+    assert np.array_equal(a[2], b[2]), "pairs"
+    assert np.array_equal(_bits(a[0]), _bits(b[0])), "pores"
+    if seed % 5 == 0 and sdf.size >= 8:
+        f = flow_fields(sdf)
+        try:
+            fa = ref.extract_network_flow(sdf, org, spc, *f[:4], grad_p_zyx=[2e-3, -1e-3, 5e-4],
+                                          ox=f[4], oy=f[5], oz=f[6])
+        except Exception:  # the reference is undefined when every voxel is labelled solid
+            return
+        fb = port.extract_network_flow(sdf, org, spc, *f[:4], grad_p_zyx=[2e-3, -1e-3, 5e-4],
+                                       ox=f[4], oy=f[5], oz=f[6])
+        assert np.array_equal(fa["throats"], fb["throats"])
+        assert np.array_equal(fa["pores"].view(np.int32), fb["pores"].view(np.int32))
+        for k in ("throat_flow", "throat_area", "pore_residual", "pore_pressure", "throat_dp"):
+            assert np.array_equal(fa[k], fb[k]), k
 
 
 def test_port_thread_count_invariance():
