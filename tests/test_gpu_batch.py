@@ -4,7 +4,7 @@ neighbours in the batch, with and without graph replay, across re-runs and capac
 import numpy as np
 import pytest
 
-from cases import edge_cases, standard_cases
+from cases import edge_cases, random_volume, standard_cases
 from oracle import sorted_pores
 from peclet_pnm_gb300 import synthetic as syn
 
@@ -42,6 +42,19 @@ def test_ragged_batch_matches_oracle(gpu, port):
     st = b.stats()
     assert st["launches"] > 0 and st["voxels"] == sum(c[1].size for c in cases)
     b.close()
+
+
+def test_random_volumes_in_one_batch_match_oracle(gpu, port):
+    """The 40 seeded random volumes (random shapes from 1 to 20 per axis, anisotropic spacing,
+    offset origins) as one ragged batch, with and without graph replay."""
+    pnm, _ = gpu
+    cases = [(f"r{s}", *random_volume(s)) for s in range(40)]
+    want = [port.extract_pore_network(sdf, org, spc) for _, sdf, org, spc in cases]
+    for graph in (True, False):
+        b = _run(pnm, cases, graph=graph)
+        for i, (name, *_rest) in enumerate(cases):
+            _check(f"{name} graph={graph}", b.result(i), want[i])
+        b.close()
 
 
 def test_batch_equals_plain_and_graph_replay(gpu):
