@@ -110,12 +110,19 @@ def test_repeated_calls_are_identical_and_reuse_workspace(gpu):
 @pytest.mark.parametrize("seed", range(40))
 def test_random_volumes_match_oracle(gpu, port, seed):
     """Seeded volumes of random shape, value family, anisotropic spacing and origin (the oracle
-    equals the reference bitwise on the same volumes): the network bit-exact, and on every fifth
-    volume the network flow within the flow bar."""
+    equals the reference bitwise on the same volumes): the network and the staged calls
+    bit-exact, and on every fifth volume the network flow within the flow bar."""
     pnm, _ = gpu
     sdf, org, spc = random_volume(seed)
     _check(pnm.extract_pore_network(sdf, org, spc, numpy=True),
            port.extract_pore_network(sdf, org, spc))
+    # the staged entry points on the same volume
+    assert np.array_equal(_bits(pnm.extract_pores(sdf, org, spc, numpy=True)),
+                          _bits(port.extract_pores(sdf, org, spc)))
+    seg = pnm.segment_volume(sdf, spc, numpy=True)
+    assert np.array_equal(seg, port.segment_volume(sdf, spc))
+    assert np.array_equal(pnm.extract_topology_gpu(seg, list(sdf.shape), numpy=True),
+                          port.extract_topology_gpu(seg, list(sdf.shape)))
     if seed % 5 == 0 and sdf.size >= 8:
         from test_gpu_flow import _check as check_flow
 
