@@ -4,7 +4,7 @@ cancellation, and that the server keeps serving after each of them."""
 import numpy as np
 import pytest
 
-from cases import edge_cases
+from cases import edge_cases, random_volume
 from oracle import sorted_pores
 from peclet_pnm_gb300 import PnmError, synthetic as syn
 from peclet_pnm_gb300._capi import PNM_ERR_ARG, PNM_ERR_CAPACITY, PNM_OK
@@ -50,6 +50,20 @@ def test_results_identical_alone_and_in_the_mix(gpu):
         st = srv.stats()  # only idle batches kept for reuse still hold memory
         assert st["running"] == 0 and st["queued"] == 0
         assert (st["bytes_in_use"] == 0) == (st["cached"] == 0)
+
+
+def test_random_volumes_served_match_oracle(gpu, port):
+    """The 40 seeded random volumes (random shapes from 1 to 20 per axis, anisotropic spacing,
+    offset origins) submitted at once, so they are coalesced into shared batches."""
+    pnm, _ = gpu
+    reqs = [random_volume(s) for s in range(40)]
+    with pnm.Server(max_inflight=2) as srv:
+        tickets = [srv.submit(*r) for r in reqs]
+        for t in tickets:
+            assert srv.wait(t, 60.0) == PNM_OK, srv.state(t)
+        for t, r in zip(tickets, reqs):
+            _same(srv.result(t), port.extract_pore_network(*r), f"ticket {t}")
+            srv.release(t)
 
 
 def test_device_resident_inputs(gpu):
