@@ -1,5 +1,5 @@
-"""The distributed surface (the reference's *_mpi functions) on CPU: two gloo ranks, each passing
-its z-slab block. The compute step is the oracle here (no GPU); what is tested is the host logic
+"""The distributed surface (the reference's *_mpi functions) on CPU: two and four gloo ranks, each
+passing its z-slab block. The compute step is the oracle here (no GPU); what is tested is the host logic
 the GPU path shares: the decomposition, the all-gather of the blocks, the pore ownership by peak
 voxel, the slicing of the labels, and that every rank's flow result is the global one."""
 import os
@@ -110,7 +110,10 @@ def test_blocks_partition_the_grid():
     assert D.mpi_block((4, 5, 6)) == ([0, 0, 0], [4, 5, 6])
 
 
-def test_two_gloo_ranks_match_the_whole_grid():
+@pytest.mark.parametrize("world", [2, 4])
+def test_gloo_ranks_match_the_whole_grid(world):
+    """2 ranks split the 21 planes 11 + 10; 4 ranks split them 6 + 5 + 5 + 5, and the third
+    block holds no pore peak, so that rank owns no pores."""
     pytest.importorskip("torch")
     import torch.multiprocessing as mp
 
@@ -121,24 +124,27 @@ def test_two_gloo_ranks_match_the_whole_grid():
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    procs = [ctx.Process(target=_rank_main, args=(r, world, port, q)) for r in range(world)]
     for p in procs:
         p.start()
-    got = sorted((q.get(timeout=300) for _ in range(2)), key=lambda g: g[0])
+    got = sorted((q.get(timeout=300) for _ in range(world)), key=lambda g: g[0])
     for p in procs:
         p.join(120)
         assert p.exitcode == 0
     sdf = _volume()
     org, spc = [0.5, -1.0, 2.0], [1.0, 1.0, 1.0]
-    wp, ws, wq = _oracle_network(sdf, org, spc)[0], *_oracle_network(sdf, org, spc)[2:]
-    assert [g[1] for g in got] == [0, 1] and all(g[2] == 2 for g in got)
+    wp, peaks, ws, wq = _oracle_network(sdf, org, spc)
+    assert [g[1] for g in got] == list(range(world)) and all(g[2] == world for g in got)
     # labels: the blocks in rank order are the whole grid's labels
-    assert got[0][3] == 0 and got[1][3] == got[0][4]
-    assert np.array_equal(np.concatenate([got[0][6], got[1][6]]), ws)
-    # pores: each owned by exactly one rank, all of them together
-    both = np.concatenate([got[0][5], got[1][5]])
+    assert got[0][3] == 0 and all(got[r][3] == got[r - 1][3] + got[r - 1][4] for r in range(1, world))
+    assert np.array_equal(np.concatenate([g[6] for g in got]), ws)
+    # pores: each rank owns those whose peak voxel lies in its block (records in voxel order)
+    pz = peaks // (sdf.shape[1] * sdf.shape[2])
+    for g in got:
+        own = wp[(pz >= g[3]) & (pz < g[3] + g[4])]
+        assert np.array_equal(sorted_pores(g[5]).view(np.int32), sorted_pores(own).view(np.int32))
+    both = np.concatenate([g[5] for g in got])
     assert np.array_equal(sorted_pores(both).view(np.int32), sorted_pores(wp).view(np.int32))
-    assert len(got[0][5]) > 0 and len(got[1][5]) > 0
     # connections and the flow result: global, the same on every rank
     for g in got:
         assert np.array_equal(g[7], wq)
