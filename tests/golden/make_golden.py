@@ -6,7 +6,8 @@ inputs and stores the outputs (and, for inputs built from transcendental functio
 ulp may differ across platforms, the inputs themselves) as compressed fixtures. The fixtures pin
 the project's C++ restatement (oracle/) on machines where the reference checkout is absent.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every fixture
+    python tests/golden/make_golden.py NAME ...   # only these
 """
 from __future__ import annotations
 
@@ -19,7 +20,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
 
+from cases import random_volume  # noqa: E402
 from oracle import Oracle, sorted_pores  # noqa: E402
 from peclet_pnm_gb300 import synthetic as syn  # noqa: E402
 
@@ -46,6 +49,11 @@ NETWORK_CASES = {
     "packing_40x48x56": (lambda: syn.packing((40, 48, 56), 0.4, seed=7), [0.0, 0.0, 0.0],
                          [1.0, 1.0, 1.0], False),
 }
+# four of the seeded random volumes of tests/cases.py, one per value family (noise, quantised
+# plateaus, noisy packing, marker-heavy), anisotropic spacing and offset origin; inputs stored
+for _s in (20, 17, 31, 34):
+    _sdf, _org, _spc = random_volume(_s)
+    NETWORK_CASES[f"random_volume_{_s}"] = (lambda v=_sdf: v, _org, _spc, True)
 
 # flow: (sdf builder, fields builder, origin_zyx, spacing_zyx, grad_p_zyx, with_openness)
 FLOW_CASES = {
@@ -63,9 +71,11 @@ FLOW_CASES = {
 }
 
 
-def main():
+def main(names=None):
     ref = Oracle("reference")
     for name, (mk, org, spc, store) in NETWORK_CASES.items():
+        if names and name not in names:
+            continue
         sdf = np.ascontiguousarray(mk(), dtype=np.float32)
         pores, seg, pairs = ref.extract_pore_network(sdf, org, spc)
         staged = ref.extract_pores(sdf, org, spc)
@@ -77,6 +87,8 @@ def main():
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
         print(f"{name}: {len(pores)} pores, {len(pairs)} pairs")
     for name, (mk, mkf, org, spc, gp, opn) in FLOW_CASES.items():
+        if names and name not in names:
+            continue
         sdf = np.ascontiguousarray(mk(), dtype=np.float32)
         f = mkf(sdf)
         kw = dict(ox=f[4], oy=f[5], oz=f[6]) if opn else {}
@@ -89,4 +101,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(set(sys.argv[1:]) or None)
