@@ -141,6 +141,76 @@ def test_port_matches_reference_random_volumes(port, seed):
             assert np.array_equal(fa[k], fb[k]), k
 
 
+_SPECIALS = np.array([np.nan, np.inf, -np.inf, 0.0, -0.0, 1.0, -1.0, -1.5, -1.4999999, -1.5000001,
+                      2.0, 1e-30, -1e-30], np.float32)
+
+
+def _fuzz_volume(rng, it):
+    """Shapes 1..6 per axis: special values only (NaN, +-inf, -0, values at the marker threshold
+    -1.5 x spacing and one ulp either side), noise with 20% special values, coarse integers
+    (plateaus), quarter-step quantised noise."""
+    shp = tuple(int(v) for v in rng.integers(1, 7, size=3))
+    mode = it % 4
+    if mode == 0:
+        a = rng.choice(_SPECIALS, size=shp)
+    elif mode == 1:
+        a = rng.normal(0, 2, size=shp).astype(np.float32)
+        m = rng.random(shp) < 0.2
+        a[m] = rng.choice(_SPECIALS, size=int(m.sum()))
+    elif mode == 2:
+        a = rng.integers(-3, 3, size=shp).astype(np.float32) * 0.5
+    else:
+        a = np.round(rng.normal(0, 1.5, size=shp) * 4) / 4
+    spc = [float(x) for x in rng.choice([0.5, 1.0, 1.0, 2.0, 0.75], size=3)]
+    org = [float(x) for x in rng.uniform(-2, 2, size=3)]
+    return np.ascontiguousarray(a, np.float32), org, spc
+
+
+@needs_ref
+@pytest.mark.parametrize("seed", range(4))
+def test_port_matches_reference_fuzz(port, seed):
+    """500 tiny volumes per seed, bitwise against the reference's own code."""
+    rng = np.random.default_rng(7000 + seed)
+    ref = Oracle("reference")
+    for it in range(500):
+        sdf, org, spc = _fuzz_volume(rng, it)
+        a = ref.extract_pore_network(sdf, org, spc)
+        b = port.extract_pore_network(sdf, org, spc)
+        assert np.array_equal(a[1], b[1]), (it, "seg")
+        assert np.array_equal(a[2], b[2]), (it, "pairs")
+        assert np.array_equal(_bits(a[0]), _bits(b[0])), (it, "pores")
+
+
+@needs_ref
+@pytest.mark.parametrize("seed", range(2))
+def test_port_flow_matches_reference_fuzz(port, seed):
+    """500 small volumes (2..8 per axis) per seed with random MAC fields, openness on every other,
+    random spacing, origin and pressure gradient: every output bitwise (same serial order)."""
+    rng = np.random.default_rng(8000 + seed)
+    ref = Oracle("reference")
+    for it in range(500):
+        shp = tuple(int(v) for v in rng.integers(2, 9, size=3))
+        sdf = rng.normal(0, 2, size=shp).astype(np.float32)
+        if it % 3 == 0:
+            sdf = (np.round(sdf * 2) / 2).astype(np.float32)
+        f = [np.ascontiguousarray(rng.normal(0, 1e-3, size=shp)) for _ in range(4)]
+        o = [np.ascontiguousarray(np.clip(rng.uniform(-0.3, 1.0, size=shp), 0, 1))
+             for _ in range(3)]
+        spc = [float(x) for x in rng.choice([0.5, 1.0, 2.0], size=3)]
+        org = [float(x) for x in rng.uniform(-2, 2, size=3)]
+        gp = [float(x) for x in rng.normal(0, 1e-3, size=3)]
+        kw = dict(ox=o[0], oy=o[1], oz=o[2]) if it % 2 else {}
+        try:
+            a = ref.extract_network_flow(sdf, org, spc, *f, grad_p_zyx=gp, **kw)
+        except Exception:  # the reference is undefined when every voxel is labelled solid
+            continue
+        b = port.extract_network_flow(sdf, org, spc, *f, grad_p_zyx=gp, **kw)
+        assert np.array_equal(a["throats"], b["throats"]), it
+        assert np.array_equal(a["pores"].view(np.int32), b["pores"].view(np.int32)), it
+        for k in ("throat_flow", "throat_area", "pore_residual", "pore_pressure", "throat_dp"):
+            assert np.array_equal(a[k], b[k]), (it, k)
+
+
 def test_port_thread_count_invariance():
     sdf = syn.packing((40, 44, 48), 0.35, seed=9)
     a = Oracle("port", threads=1).extract_pore_network(sdf, [0, 0, 0], [1, 1, 1])
