@@ -182,6 +182,25 @@ def test_port_matches_reference_fuzz(port, seed):
 
 
 @needs_ref
+def test_port_staged_calls_match_reference_fuzz(port):
+    """The staged calls on 500 fuzzed tiny volumes, and the topology of random labels."""
+    rng = np.random.default_rng(7500)
+    ref = Oracle("reference")
+    for it in range(500):
+        sdf, org, spc = _fuzz_volume(rng, it)
+        assert np.array_equal(_bits(ref.extract_pores(sdf, org, spc)),
+                              _bits(port.extract_pores(sdf, org, spc))), it
+        seg = ref.segment_volume(sdf, spc)
+        assert np.array_equal(seg, port.segment_volume(sdf, spc)), it
+        shape = list(sdf.shape)
+        assert np.array_equal(ref.extract_topology_gpu(seg, shape),
+                              port.extract_topology_gpu(seg, shape)), it
+        lab = rng.integers(-4, 5, size=sdf.size).astype(np.int32)
+        assert np.array_equal(ref.extract_topology_gpu(lab, shape),
+                              port.extract_topology_gpu(lab, shape)), it
+
+
+@needs_ref
 @pytest.mark.parametrize("seed", range(2))
 def test_port_flow_matches_reference_fuzz(port, seed):
     """500 small volumes (2..8 per axis) per seed with random MAC fields, openness on every other,
