@@ -8,7 +8,9 @@ WholeExtent is one larger than the arrays). Each case stores the file bytes and 
 returned. Writer: scripts/vti.py save_vti is imported from the reference checkout and its output
 for a small labelled volume is stored byte for byte.
 
-    PNM_REFERENCE=<reference checkout> python tests/golden/make_vti_golden.py
+    PNM_REFERENCE=<reference checkout> python tests/golden/make_vti_golden.py [--writer-extra]
+
+(--writer-extra: only the eight extra writer cases, tests/golden/vti/writer_cases.npz)
 """
 from __future__ import annotations
 
@@ -78,6 +80,43 @@ def writer_case(rng, mod) -> bytes:
         return fields, open(p, "rb").read()
 
 
+def extra_writer_cases(rng, mod) -> dict:
+    """Eight more field sets through the reference writer: every integer width (written as
+    Int32), float16 / float32 / float64, bool, vector fields, integer spacing (formatted without
+    a decimal point) and float origins."""
+    dts = [np.int8, np.uint8, np.int16, np.int64, np.uint32, np.float16, np.float32, np.float64,
+           np.bool_]
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        for i in range(8):
+            shp = tuple(int(v) for v in rng.integers(1, 5, size=3))
+            names = []
+            for j in range(1 + i % 3):
+                dt = dts[(3 * i + j) % len(dts)]
+                s = shp + ((3,) if (i + j) % 3 == 0 else ())
+                if np.issubdtype(dt, np.floating):
+                    arr = rng.normal(0, 10, size=s).astype(dt)
+                else:
+                    arr = rng.integers(-50, 50, size=s).astype(dt)
+                name = ["Labels", "SDF", "vel"][j] + str(i)
+                names.append(name)
+                out[f"w{i}__f{j}"] = arr
+            int_spacing = i % 4 == 0
+            spacing = (tuple(int(v) for v in rng.integers(1, 4, size=3)) if int_spacing else
+                       tuple(float(v) for v in rng.choice([0.5, 0.1, 1e-3, 2.0, 0.30000001],
+                                                          size=3)))
+            origin = tuple(float(v) for v in rng.normal(0, 5, size=3))
+            p = os.path.join(d, "w.vti")
+            mod.save_vti(p, {n: out[f"w{i}__f{j}"] for j, n in enumerate(names)},
+                         spacing=spacing, origin=origin)
+            out[f"w{i}__names"] = np.array(names)
+            out[f"w{i}__spacing"] = np.array(spacing, np.float64)
+            out[f"w{i}__int_spacing"] = np.array(int_spacing)
+            out[f"w{i}__origin"] = np.array(origin, np.float64)
+            out[f"w{i}__bytes"] = np.frombuffer(open(p, "rb").read(), np.uint8)
+    return out
+
+
 def main():
     if not os.path.exists(os.path.join(REF, "scripts", "vti.py")):
         sys.stderr.write("set PNM_REFERENCE to the reference checkout\n")
@@ -113,8 +152,12 @@ def main():
     for k, a in fields.items():
         out[f"writer__field__{k}"] = a
     out["writer__bytes"] = np.frombuffer(wbytes, np.uint8)
-    np.savez_compressed(os.path.join(HERE, "vti", "cases.npz"), **out)
-    print(f"wrote {len(cases)} reader cases and one writer case")
+    if "--writer-extra" not in sys.argv:
+        np.savez_compressed(os.path.join(HERE, "vti", "cases.npz"), **out)
+        print(f"wrote {len(cases)} reader cases and one writer case")
+    extra = extra_writer_cases(np.random.default_rng(20261204), mod)
+    np.savez_compressed(os.path.join(HERE, "vti", "writer_cases.npz"), **extra)
+    print("wrote 8 more writer cases")
 
 
 if __name__ == "__main__":

@@ -46,6 +46,24 @@ def test_save_vti_matches_reference_writer(tmp_path):
     assert p.read_bytes() == GOLDEN["writer__bytes"].tobytes()
 
 
+WRITER = np.load(os.path.join(os.path.dirname(__file__), "golden", "vti", "writer_cases.npz"))
+
+
+@pytest.mark.parametrize("i", range(8))
+def test_save_vti_matches_reference_writer_more(tmp_path, i):
+    """Every integer width (written as Int32), float16 / 32 / 64, bool, vector fields, integer
+    spacing and float origins, against the reference writer's bytes."""
+    names = [str(n) for n in WRITER[f"w{i}__names"]]
+    fields = {n: WRITER[f"w{i}__f{j}"] for j, n in enumerate(names)}
+    sp = WRITER[f"w{i}__spacing"]
+    spacing = tuple(int(v) for v in sp) if bool(WRITER[f"w{i}__int_spacing"]) else \
+        tuple(float(v) for v in sp)
+    origin = tuple(float(v) for v in WRITER[f"w{i}__origin"])
+    p = tmp_path / "w.vti"
+    pnm.save_vti(str(p), fields, spacing=spacing, origin=origin)
+    assert p.read_bytes() == WRITER[f"w{i}__bytes"].tobytes()
+
+
 @pytest.mark.parametrize("shape", [(1, 1, 1), (3, 5, 7), (16, 9, 33), (40, 2, 1)])
 def test_round_trip(tmp_path, shape):
     rng = np.random.default_rng(sum(shape))
